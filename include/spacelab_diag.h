@@ -1,0 +1,26 @@
+/*
+ * spacelab_diag.h -- diagnostics of libspacelab_gb300.so (no counterpart in
+ * the reference): device-side checks and measurements used by the tests
+ * and the benchmark.  Not needed to run a simulation.
+ */
+#ifndef SPACELAB_DIAG_H
+#define SPACELAB_DIAG_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* For i < n computes on the current GPU q_recip[i] = the step kernels'
+ * reciprocal-based quotient of a[i] / b[i] (b[i] > 0, with RN(1/b[i])) and
+ * q_ieee[i] = the IEEE double quotient a[i] / b[i].  Host arrays. */
+int sl_diag_division(int n, const double* a, const double* b, double* q_recip, double* q_ieee);
+
+/* Measured FP64 fused-multiply-add throughput of the current GPU in
+ * GFLOP/s (2 flops per FMA), from a kernel of independent FMA chains timed
+ * with CUDA events. */
+int sl_diag_fp64_peak(double* gflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SPACELAB_DIAG_H */

@@ -1,0 +1,477 @@
+// sl_capi.cu -- the extern "C" handle API of include/spacelab_gpu.h.
+//
+// A handle owns one device arena holding the structure-of-arrays state of
+// one system, the per-pair scratch (pairbuf/torqbuf/cmask) and the energy
+// reduction buffers, plus a CUDA stream and, for sl_run, an instantiated
+// CUDA graph of one write interval.  All host<->device copies go through a
+// pinned staging buffer that also performs the AoS (vec3[n]) <-> SoA
+// transposition.
+#include "../../include/spacelab_gpu.h"
+#include "sl_device.cuh"
+#include "sl_kernels.h"
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+namespace {
+
+thread_local std::string g_last_error = "";
+
+int fail(int code, const std::string& msg)
+{
+    g_last_error = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what)
+{
+    return fail(SL_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define SL_CUDA(call)                                  \
+    do {                                               \
+        cudaError_t e_ = (call);                       \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+    } while (0)
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+constexpr int kTimerPool = 8192;
+
+}  // namespace
+
+struct sl_handle {
+    sl::System sys{};
+    sl::Scalars host_sc{0, 0, 0};
+    sl::Scalars* d_sc = nullptr;
+    int mode = SL_MODE_EXACT;
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    void* arena = nullptr;
+    size_t arena_bytes = 0;
+    double* staging = nullptr;  // pinned, 18 * npad doubles
+    double* h_energy = nullptr; // pinned, 8 doubles
+    unsigned int* h_status = nullptr;
+    bool uploaded = false;
+    bool forces_ready = false;
+    // graph of one write interval for sl_run
+    cudaGraphExec_t interval_exec = nullptr;
+    int interval_skip = 0;
+    // kernel timing
+    bool timing = false;
+    std::vector<sl::StepTimers> timers;
+    int timers_used = 0;
+    double pair_ms = 0, rowsum_ms = 0;
+    long launches = 0;
+};
+
+namespace {
+
+int check_handle(const sl_handle* h)
+{
+    if (!h) return fail(SL_ERR_ARG, "null handle");
+    return SL_OK;
+}
+
+// One step on the handle's stream, with optional timing events.
+int enqueue_step(sl_handle* h, bool write)
+{
+    sl::StepTimers* tm = nullptr;
+    if (h->timing) {
+        if (h->timers_used >= (int)h->timers.size()) {
+            sl::StepTimers t;
+            for (int k = 0; k < 3; ++k) SL_CUDA(cudaEventCreate(&t.ev[k]));
+            if ((int)h->timers.size() >= kTimerPool) return fail(SL_ERR_STATE, "timer pool exhausted; read sl_kernel_times");
+            h->timers.push_back(t);
+        }
+        tm = &h->timers[h->timers_used++];
+    }
+    sl::launch_step(h->sys, write, h->num_sms, h->stream, tm);
+    SL_CUDA(cudaGetLastError());
+    return SL_OK;
+}
+
+int fetch_energy_and_status(sl_handle* h, sl_energy* out, bool want_energy)
+{
+    if (want_energy)
+        SL_CUDA(cudaMemcpyAsync(h->h_energy, h->sys.energy, 8 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    SL_CUDA(cudaMemcpyAsync(h->h_status, h->sys.status, sizeof(unsigned int), cudaMemcpyDeviceToHost, h->stream));
+    SL_CUDA(cudaStreamSynchronize(h->stream));
+    if (want_energy && out) {
+        out->PE = h->h_energy[0];
+        out->KE = h->h_energy[1];
+        for (int k = 0; k < 3; ++k) {
+            out->mom[k] = h->h_energy[2 + k];
+            out->ang_mom[k] = h->h_energy[5 + k];
+        }
+    }
+    if (*h->h_status) return fail(SL_ERR_NONFINITE, "state became non-finite (NaN/Inf position, velocity or spin)");
+    return SL_OK;
+}
+
+// AoS vec3[n] -> staging SoA rows (3 x npad) -> device Vec3Soa.
+int put_vec3(sl_handle* h, const double* aos, const sl::Vec3Soa& dst, double* stage)
+{
+    const int n = h->sys.n, np = h->sys.npad;
+    for (int c = 0; c < 3; ++c) {
+        double* row = stage + (size_t)c * np;
+        for (int i = 0; i < n; ++i) row[i] = aos ? aos[3 * (size_t)i + c] : 0.0;
+        for (int i = n; i < np; ++i) row[i] = 0.0;
+        SL_CUDA(cudaMemcpyAsync(dst.c[c], row, np * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    }
+    return SL_OK;
+}
+
+int get_vec3(sl_handle* h, const sl::Vec3Soa& src, double* stage)
+{
+    const int np = h->sys.npad;
+    for (int c = 0; c < 3; ++c)
+        SL_CUDA(cudaMemcpyAsync(stage + (size_t)c * np, src.c[c], np * sizeof(double), cudaMemcpyDeviceToHost,
+                                h->stream));
+    return SL_OK;
+}
+
+void unstage_vec3(const sl_handle* h, const double* stage, double* aos)
+{
+    const int n = h->sys.n, np = h->sys.npad;
+    for (int c = 0; c < 3; ++c)
+        for (int i = 0; i < n; ++i) aos[3 * (size_t)i + c] = stage[(size_t)c * np + i];
+}
+
+void drop_graph(sl_handle* h)
+{
+    if (h->interval_exec) cudaGraphExecDestroy(h->interval_exec);
+    h->interval_exec = nullptr;
+    h->interval_skip = 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sl_version(void) { return SL_API_VERSION; }
+
+const char* sl_last_error(void) { return g_last_error.c_str(); }
+
+int sl_create(int n, const sl_material* mat, int mode, sl_handle** out)
+{
+    if (!out) return fail(SL_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    if (n < 1) return fail(SL_ERR_ARG, "n must be >= 1");
+    if (n > 46340) return fail(SL_ERR_ARG, "n > 46340 exceeds the reference's pair index range");
+    if (!mat) return fail(SL_ERR_ARG, "material is NULL");
+    if (mode != SL_MODE_EXACT) return fail(SL_ERR_UNSUPPORTED, "unknown mode");
+    if (!(mat->h_min > 0)) return fail(SL_ERR_ARG, "h_min must be > 0");
+
+    sl_handle* h = new (std::nothrow) sl_handle();
+    if (!h) return fail(SL_ERR_ALLOC, "host allocation failed");
+    h->mode = mode;
+    cudaError_t e = cudaGetDevice(&h->device);
+    if (e != cudaSuccess) { delete h; return cuda_fail(e, "cudaGetDevice"); }
+    e = cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
+    if (e != cudaSuccess) { delete h; return cuda_fail(e, "cudaDeviceGetAttribute"); }
+    e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { delete h; return cuda_fail(e, "cudaStreamCreate"); }
+
+    sl::System& s = h->sys;
+    s.n = n;
+    s.npad = (n + sl::kBlock - 1) / sl::kBlock * sl::kBlock;
+    s.nb = s.npad / sl::kBlock;
+    s.ntiles = (long long)s.nb * (s.nb + 1) / 2;
+    s.mat = sl::Material{mat->G, mat->Ha, mat->u_s, mat->u_r, mat->h_min};
+    const size_t np = s.npad;
+    const size_t A = 256;
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off = align_up(off + bytes, A); return o; };
+    size_t o_vec[8][3];
+    for (int v = 0; v < 8; ++v)
+        for (int c = 0; c < 3; ++c) o_vec[v][c] = take(np * sizeof(double));
+    size_t o_sc[8];
+    for (int k = 0; k < 8; ++k) o_sc[k] = take(np * sizeof(double));
+    const size_t o_pair = take(3 * np * np * sizeof(double));
+    const size_t o_torq = take(3 * np * np * sizeof(double));
+    const size_t o_mask = take(np * s.nb * sizeof(uint32_t));
+    const size_t o_pe = take((size_t)s.ntiles * sizeof(double));
+    const size_t o_red = take(sl::kRedBlocks * 8 * sizeof(double));
+    const size_t o_en = take(8 * sizeof(double));
+    const size_t o_st = take(sizeof(unsigned int));
+    const size_t o_scl = take(sizeof(sl::Scalars));
+    h->arena_bytes = off;
+    e = cudaMalloc(&h->arena, h->arena_bytes);
+    if (e != cudaSuccess) { sl_destroy(h); return fail(SL_ERR_ALLOC, std::string("cudaMalloc: ") + cudaGetErrorString(e)); }
+    char* base = static_cast<char*>(h->arena);
+    sl::Vec3Soa* vecs[8] = {&s.pos, &s.prev, &s.vel, &s.velh, &s.w, &s.wh, &s.acc, &s.aacc};
+    for (int v = 0; v < 8; ++v)
+        for (int c = 0; c < 3; ++c) vecs[v]->c[c] = reinterpret_cast<double*>(base + o_vec[v][c]);
+    double** scal[8] = {&s.R, &s.m, &s.moi, &s.twoR, &s.fourR, &s.cR3, &s.inv_m, &s.inv_moi};
+    for (int k = 0; k < 8; ++k) *scal[k] = reinterpret_cast<double*>(base + o_sc[k]);
+    s.pairbuf = reinterpret_cast<double*>(base + o_pair);
+    s.torqbuf = reinterpret_cast<double*>(base + o_torq);
+    s.cmask = reinterpret_cast<uint32_t*>(base + o_mask);
+    s.pe_tile = reinterpret_cast<double*>(base + o_pe);
+    s.red = reinterpret_cast<double*>(base + o_red);
+    s.energy = reinterpret_cast<double*>(base + o_en);
+    s.status = reinterpret_cast<unsigned int*>(base + o_st);
+    h->d_sc = reinterpret_cast<sl::Scalars*>(base + o_scl);
+    s.sc = h->d_sc;
+    e = cudaMemsetAsync(h->arena, 0, h->arena_bytes, h->stream);
+    if (e != cudaSuccess) { sl_destroy(h); return cuda_fail(e, "cudaMemset"); }
+    e = cudaMallocHost(&h->staging, 18 * np * sizeof(double));
+    if (e == cudaSuccess) e = cudaMallocHost(&h->h_energy, 8 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMallocHost(&h->h_status, sizeof(unsigned int));
+    if (e != cudaSuccess) { sl_destroy(h); return fail(SL_ERR_ALLOC, "pinned host allocation failed"); }
+    e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) { sl_destroy(h); return cuda_fail(e, "cudaStreamSynchronize"); }
+    *out = h;
+    return SL_OK;
+}
+
+int sl_destroy(sl_handle* h)
+{
+    if (!h) return SL_OK;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    drop_graph(h);
+    for (auto& t : h->timers)
+        for (int k = 0; k < 3; ++k) cudaEventDestroy(t.ev[k]);
+    if (h->arena) cudaFree(h->arena);
+    if (h->staging) cudaFreeHost(h->staging);
+    if (h->h_energy) cudaFreeHost(h->h_energy);
+    if (h->h_status) cudaFreeHost(h->h_status);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return SL_OK;
+}
+
+int sl_num_particles(const sl_handle* h, int* n)
+{
+    if (int r = check_handle(h)) return r;
+    if (!n) return fail(SL_ERR_ARG, "n is NULL");
+    *n = h->sys.n;
+    return SL_OK;
+}
+
+int sl_upload(sl_handle* h, const double* pos, const double* vel, const double* w, const double* R,
+              const double* m, const double* moi)
+{
+    if (int r = check_handle(h)) return r;
+    if (!R || !m || !moi) return fail(SL_ERR_ARG, "R, m or moi is NULL");
+    const int n = h->sys.n, np = h->sys.npad;
+    for (int i = 0; i < n; ++i) {
+        if (!(R[i] > 0) || !(m[i] > 0) || !(moi[i] > 0) || !std::isfinite(R[i]) || !std::isfinite(m[i]) ||
+            !std::isfinite(moi[i]))
+            return fail(SL_ERR_ARG, "R, m and moi must be finite and > 0 (sphere " + std::to_string(i) + ")");
+    }
+    if (int r = sl_upload_resume(h, pos, vel, w, nullptr, nullptr, nullptr)) return r;
+    // padded spheres get R = m = moi = 1 (they are never paired)
+    const double* src[3] = {R, m, moi};
+    double* dst[3] = {h->sys.R, h->sys.m, h->sys.moi};
+    for (int k = 0; k < 3; ++k) {
+        double* row = h->staging + (size_t)k * np;
+        for (int i = 0; i < n; ++i) row[i] = src[k][i];
+        for (int i = n; i < np; ++i) row[i] = 1.0;
+        SL_CUDA(cudaMemcpyAsync(dst[k], row, np * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    }
+    sl::launch_derive(h->sys, h->stream);
+    SL_CUDA(cudaGetLastError());
+    SL_CUDA(cudaStreamSynchronize(h->stream));
+    h->uploaded = true;
+    h->forces_ready = false;
+    return SL_OK;
+}
+
+int sl_upload_resume(sl_handle* h, const double* pos, const double* vel, const double* w, const double* acc,
+                     const double* aacc, const double* pos_prev)
+{
+    if (int r = check_handle(h)) return r;
+    if (!pos || !vel || !w) return fail(SL_ERR_ARG, "pos, vel or w is NULL");
+    const int n = h->sys.n;
+    for (int i = 0; i < 3 * n; ++i)
+        if (!std::isfinite(pos[i]) || !std::isfinite(vel[i]) || !std::isfinite(w[i]))
+            return fail(SL_ERR_ARG, "non-finite position, velocity or spin in input");
+    const size_t np = h->sys.npad;
+    double* st = h->staging;
+    // each array has its own staging rows (copies are asynchronous)
+    const double* srcs[6] = {pos, vel, w, acc, aacc, pos_prev ? pos_prev : pos};
+    const sl::Vec3Soa* dsts[6] = {&h->sys.pos, &h->sys.vel, &h->sys.w, &h->sys.acc, &h->sys.aacc, &h->sys.prev};
+    for (int k = 0; k < 6; ++k) {
+        if (int r = put_vec3(h, srcs[k], *dsts[k], st + (size_t)(3 * k) * np)) return r;
+    }
+    SL_CUDA(cudaMemsetAsync(h->sys.status, 0, sizeof(unsigned int), h->stream));
+    SL_CUDA(cudaStreamSynchronize(h->stream));
+    h->forces_ready = (acc != nullptr && aacc != nullptr);
+    return SL_OK;
+}
+
+int sl_set_scalars(sl_handle* h, double dt, double kin, double kout)
+{
+    if (int r = check_handle(h)) return r;
+    if (!std::isfinite(dt) || !std::isfinite(kin) || !std::isfinite(kout) || dt < 0 || kin < 0 || kout < 0)
+        return fail(SL_ERR_ARG, "dt, kin, kout must be finite and >= 0");
+    h->host_sc = sl::Scalars{dt, kin, kout};
+    SL_CUDA(cudaMemcpyAsync(h->d_sc, &h->host_sc, sizeof(sl::Scalars), cudaMemcpyHostToDevice, h->stream));
+    SL_CUDA(cudaStreamSynchronize(h->stream));
+    return SL_OK;
+}
+
+int sl_init_forces(sl_handle* h, sl_energy* out)
+{
+    if (int r = check_handle(h)) return r;
+    if (!h->uploaded) return fail(SL_ERR_STATE, "sl_upload first");
+    // A step with dt = 0 leaves pos/vel/w unchanged, sets prev = pos and
+    // evaluates the pair terms of init_conditions, with the energy totals.
+    const sl::Scalars zero{0.0, h->host_sc.kin, h->host_sc.kout};
+    SL_CUDA(cudaMemcpyAsync(h->d_sc, &zero, sizeof(sl::Scalars), cudaMemcpyHostToDevice, h->stream));
+    for (int c = 0; c < 3; ++c) {
+        SL_CUDA(cudaMemsetAsync(h->sys.acc.c[c], 0, h->sys.npad * sizeof(double), h->stream));
+        SL_CUDA(cudaMemsetAsync(h->sys.aacc.c[c], 0, h->sys.npad * sizeof(double), h->stream));
+    }
+    if (int r = enqueue_step(h, true)) return r;
+    SL_CUDA(cudaMemcpyAsync(h->d_sc, &h->host_sc, sizeof(sl::Scalars), cudaMemcpyHostToDevice, h->stream));
+    const int r = fetch_energy_and_status(h, out, true);
+    h->forces_ready = (r == SL_OK);
+    return r;
+}
+
+int sl_step(sl_handle* h, int nsteps, int write_last, sl_energy* out)
+{
+    if (int r = check_handle(h)) return r;
+    if (!h->uploaded) return fail(SL_ERR_STATE, "sl_upload first");
+    if (nsteps < 0) return fail(SL_ERR_ARG, "nsteps < 0");
+    for (int k = 0; k < nsteps; ++k)
+        if (int r = enqueue_step(h, write_last && k == nsteps - 1)) return r;
+    return fetch_energy_and_status(h, out, write_last && nsteps > 0);
+}
+
+int sl_run(sl_handle* h, int first_step, int last_step, int skip, sl_energy* rows, int max_rows, int* nrows)
+{
+    if (int r = check_handle(h)) return r;
+    if (!h->uploaded) return fail(SL_ERR_STATE, "sl_upload first");
+    if (skip < 1) return fail(SL_ERR_ARG, "skip must be >= 1 (ColliderSingleCore.cpp:402-405)");
+    if (first_step < 1 || last_step < first_step) return fail(SL_ERR_ARG, "need 1 <= first_step <= last_step");
+    if (nrows) *nrows = 0;
+    int written = 0;
+    int step = first_step;
+    const bool use_graph = !h->timing;
+    while (step < last_step) {
+        if (use_graph && skip > 1 && (step - 1) % skip == 0 && step + skip - 1 < last_step) {
+            // a whole interval: skip-1 plain steps then one write step
+            if (h->interval_skip != skip) {
+                drop_graph(h);
+                cudaGraph_t g;
+                SL_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+                for (int k = 0; k < skip; ++k) sl::launch_step(h->sys, k == skip - 1, h->num_sms, h->stream, nullptr);
+                SL_CUDA(cudaStreamEndCapture(h->stream, &g));
+                const cudaError_t e = cudaGraphInstantiate(&h->interval_exec, g, 0);
+                cudaGraphDestroy(g);
+                if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+                h->interval_skip = skip;
+            }
+            SL_CUDA(cudaGraphLaunch(h->interval_exec, h->stream));
+            step += skip;
+            const int r = fetch_energy_and_status(h, written < max_rows && rows ? &rows[written] : nullptr, true);
+            if (r) { if (nrows) *nrows = written; return r; }
+            if (written < max_rows) ++written;
+        } else {
+            const bool write = (step % skip == 0);
+            if (int r = enqueue_step(h, write)) return r;
+            if (write) {
+                const int r = fetch_energy_and_status(h, written < max_rows && rows ? &rows[written] : nullptr, true);
+                if (r) { if (nrows) *nrows = written; return r; }
+                if (written < max_rows) ++written;
+            }
+            ++step;
+        }
+    }
+    if (nrows) *nrows = written;
+    return fetch_energy_and_status(h, nullptr, false);
+}
+
+int sl_download(sl_handle* h, double* pos, double* vel, double* w, double* acc, double* aacc)
+{
+    if (int r = check_handle(h)) return r;
+    double* outs[5] = {pos, vel, w, acc, aacc};
+    const sl::Vec3Soa* srcs[5] = {&h->sys.pos, &h->sys.vel, &h->sys.w, &h->sys.acc, &h->sys.aacc};
+    const size_t np = h->sys.npad;
+    for (int k = 0; k < 5; ++k)
+        if (outs[k])
+            if (int r = get_vec3(h, *srcs[k], h->staging + 3 * k * np)) return r;
+    SL_CUDA(cudaStreamSynchronize(h->stream));
+    for (int k = 0; k < 5; ++k)
+        if (outs[k]) unstage_vec3(h, h->staging + 3 * k * np, outs[k]);
+    return SL_OK;
+}
+
+int sl_contacts(sl_handle* h, int* pairs, long max_pairs, long* count)
+{
+    if (int r = check_handle(h)) return r;
+    if (!count) return fail(SL_ERR_ARG, "count is NULL");
+    if (!h->forces_ready) return fail(SL_ERR_STATE, "no force pass has run");
+    const sl::System& s = h->sys;
+    std::vector<uint32_t> mask((size_t)s.npad * s.nb);
+    SL_CUDA(cudaMemcpyAsync(mask.data(), s.cmask, mask.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
+    SL_CUDA(cudaStreamSynchronize(h->stream));
+    long c = 0;
+    for (int A = 0; A < s.n; ++A) {
+        for (int Y = 0; Y <= A / sl::kBlock; ++Y) {
+            uint32_t wd = mask[(size_t)A * s.nb + Y];
+            while (wd) {
+                const int b = __builtin_ctz(wd);
+                wd &= wd - 1;
+                const int B = Y * sl::kBlock + b;
+                if (B >= A) break;
+                if (pairs && c < max_pairs) { pairs[2 * c] = A; pairs[2 * c + 1] = B; }
+                ++c;
+            }
+        }
+    }
+    *count = c;
+    return SL_OK;
+}
+
+void* sl_stream(sl_handle* h) { return h ? static_cast<void*>(h->stream) : nullptr; }
+
+int sl_kernel_timing(sl_handle* h, int enable)
+{
+    if (int r = check_handle(h)) return r;
+    SL_CUDA(cudaStreamSynchronize(h->stream));
+    h->timing = enable != 0;
+    h->timers_used = 0;
+    h->pair_ms = h->rowsum_ms = 0;
+    h->launches = 0;
+    return SL_OK;
+}
+
+int sl_kernel_times(sl_handle* h, double* pair_ms, double* rowsum_ms, long* launches, int reset)
+{
+    if (int r = check_handle(h)) return r;
+    SL_CUDA(cudaStreamSynchronize(h->stream));
+    for (int k = 0; k < h->timers_used; ++k) {
+        float a = 0, b = 0;
+        SL_CUDA(cudaEventElapsedTime(&a, h->timers[k].ev[0], h->timers[k].ev[1]));
+        SL_CUDA(cudaEventElapsedTime(&b, h->timers[k].ev[1], h->timers[k].ev[2]));
+        h->pair_ms += a;
+        h->rowsum_ms += b;
+        h->launches += 1;
+    }
+    h->timers_used = 0;
+    if (pair_ms) *pair_ms = h->pair_ms;
+    if (rowsum_ms) *rowsum_ms = h->rowsum_ms;
+    if (launches) *launches = h->launches;
+    if (reset) { h->pair_ms = h->rowsum_ms = 0; h->launches = 0; }
+    return SL_OK;
+}
+
+int sl_device_bytes(const sl_handle* h, uint64_t* bytes)
+{
+    if (int r = check_handle(h)) return r;
+    if (!bytes) return fail(SL_ERR_ARG, "bytes is NULL");
+    *bytes = h->arena_bytes;
+    return SL_OK;
+}
+
+}  // extern "C"

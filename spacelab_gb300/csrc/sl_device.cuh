@@ -1,0 +1,87 @@
+// sl_device.cuh -- device-side data layout and arithmetic helpers shared by
+// the step kernels.
+//
+// HBM layout of one system (all arrays are structure-of-arrays, padded to
+// npad = ceil(n / 32) * 32 spheres so that every 32-sphere block is whole):
+//   pos, prev, vel, velh, w, wh, acc, aacc   [3][npad] doubles (x, y, z rows)
+//   R, m, moi                                [npad]
+//   twoR = 2R, fourR = 4R                    exact power-of-two scalings
+//   cR3  = ((Ha/6*64)*R)*R*R                 the sphere-A prefix of the vdW
+//                                            coefficient chain
+//   inv_m = RN(1/m), inv_moi = RN(1/moi)     correctly rounded reciprocals
+//   pairbuf[3][npad][npad]                   per-pair force contributions,
+//                                            row s holds the terms that sphere
+//                                            s adds to acc[s] (scratch)
+//   torqbuf[3][npad][npad]                   per-pair torque contributions,
+//                                            written only for contacts
+//   cmask[npad][nb]                          contact bit per (s, 32-block)
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace sl {
+
+constexpr int kBlock = 32;  // spheres per pair tile edge (one warp lane each)
+
+struct Material {
+    double G, Ha, u_s, u_r, h_min;
+};
+
+// Per-step scalars live in device memory so that captured CUDA graphs stay
+// valid when the host changes dt or the spring constants.
+struct Scalars {
+    double dt, kin, kout;
+};
+
+struct Vec3Soa {
+    double* c[3];
+};
+
+struct System {
+    int n, npad, nb;
+    long long ntiles;  // nb * (nb + 1) / 2 lower-triangular block tiles
+    Vec3Soa pos, prev, vel, velh, w, wh, acc, aacc;
+    double *R, *m, *moi, *twoR, *fourR, *cR3, *inv_m, *inv_moi;
+    double* pairbuf;      // [3][npad][npad]
+    double* torqbuf;      // [3][npad][npad]
+    uint32_t* cmask;      // [npad][nb]
+    double* pe_tile;      // [ntiles]
+    double* red;          // [kRedBlocks][8] energy partials
+    double* energy;       // [8] PE, KE, mom xyz, L xyz
+    unsigned int* status; // error bits (see SL_ERR_* in spacelab_gpu.h)
+    const Scalars* sc;
+    Material mat;
+};
+
+// Correctly rounded quotient a / b given y = RN(1/b) (b > 0, normal range).
+// Two residual corrections after q0 = RN(a*y), following Markstein's
+// theorem for FMA-based division (P. Markstein, "Computation of elementary
+// functions on the IBM RISC System/6000 processor", IBM J. Res. Dev. 34(1),
+// 1990; see also Muller et al., Handbook of Floating-Point Arithmetic,
+// ch. "Division"):
+//   q1 = q0 + (a - b q0) y   is a faithful rounding of a/b,
+//   q2 = q1 + (a - b q1) y   with exact residual, equals RN(a/b) because
+//   |q1 + r1 y - a/b| <= |a/b - q1| * |1 - b y| < (ulp/2 + d) u, and a
+//   quotient of two 53-bit numbers is more than 2^-54 ulp from any midpoint.
+// Five FP64 pipe operations instead of a full division; tested bit-for-bit
+// against IEEE division in tests/test_gpu_division.py.
+__device__ __forceinline__ double div_by_recip(double a, double b, double y)
+{
+    const double q0 = a * y;
+    const double r0 = fma(-b, q0, a);
+    const double q1 = fma(r0, y, q0);
+    const double r1 = fma(-b, q1, a);
+    return fma(r1, y, q1);
+}
+
+// Lower-triangular tile index t -> (X, Y), X >= Y, t = X(X+1)/2 + Y.
+__device__ __forceinline__ void tile_coords(long long t, int& X, int& Y)
+{
+    long long x = (long long)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+    while (x * (x + 1) / 2 > t) --x;
+    while ((x + 1) * (x + 2) / 2 <= t) ++x;
+    X = (int)x;
+    Y = (int)(t - x * (x + 1) / 2);
+}
+
+}  // namespace sl

@@ -1,0 +1,93 @@
+// sl_diag.cu -- diagnostics (include/spacelab_diag.h).
+#include "../../include/spacelab_diag.h"
+#include "../../include/spacelab_gpu.h"
+#include "sl_device.cuh"
+
+#include <cuda_runtime.h>
+
+namespace {
+
+__global__ void division_kernel(int n, const double* a, const double* b, double* qr, double* qi)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double y = 1.0 / b[i];
+    qr[i] = sl::div_by_recip(a[i], b[i], y);
+    qi[i] = a[i] / b[i];
+}
+
+constexpr int kChains = 8;
+constexpr int kIters = 4096;
+
+__global__ void fma_chain_kernel(double* out, double seed)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[kChains];
+#pragma unroll
+    for (int k = 0; k < kChains; ++k) v[k] = seed + t * 1e-9 + k;
+    const double b = 0.999999, c = 1e-7;
+    for (int i = 0; i < kIters; ++i) {
+#pragma unroll
+        for (int k = 0; k < kChains; ++k) v[k] = fma(v[k], b, c);
+    }
+    double s = 0;
+#pragma unroll
+    for (int k = 0; k < kChains; ++k) s += v[k];
+    out[t] = s;
+}
+
+}  // namespace
+
+extern "C" int sl_diag_division(int n, const double* a, const double* b, double* q_recip, double* q_ieee)
+{
+    if (n < 1 || !a || !b || !q_recip || !q_ieee) return SL_ERR_ARG;
+    double* d = nullptr;
+    const size_t bytes = (size_t)n * sizeof(double);
+    if (cudaMalloc(&d, 4 * bytes) != cudaSuccess) return SL_ERR_ALLOC;
+    int rc = SL_OK;
+    if (cudaMemcpy(d, a, bytes, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(d + n, b, bytes, cudaMemcpyHostToDevice) != cudaSuccess)
+        rc = SL_ERR_CUDA;
+    if (rc == SL_OK) {
+        division_kernel<<<(n + 255) / 256, 256>>>(n, d, d + n, d + 2 * (size_t)n, d + 3 * (size_t)n);
+        if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) rc = SL_ERR_CUDA;
+    }
+    if (rc == SL_OK && (cudaMemcpy(q_recip, d + 2 * (size_t)n, bytes, cudaMemcpyDeviceToHost) != cudaSuccess ||
+                        cudaMemcpy(q_ieee, d + 3 * (size_t)n, bytes, cudaMemcpyDeviceToHost) != cudaSuccess))
+        rc = SL_ERR_CUDA;
+    cudaFree(d);
+    return rc;
+}
+
+extern "C" int sl_diag_fp64_peak(double* gflops)
+{
+    if (!gflops) return SL_ERR_ARG;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return SL_ERR_CUDA;
+    const int blocks = sms * 8, threads = 256;
+    double* out = nullptr;
+    if (cudaMalloc(&out, (size_t)blocks * threads * sizeof(double)) != cudaSuccess) return SL_ERR_ALLOC;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    int rc = SL_OK;
+    for (int rep = 0; rep < 4 && rc == SL_OK; ++rep) {
+        cudaEventRecord(e0);
+        fma_chain_kernel<<<blocks, threads>>>(out, 1.0);
+        cudaEventRecord(e1);
+        if (cudaEventSynchronize(e1) != cudaSuccess || cudaGetLastError() != cudaSuccess) rc = SL_ERR_CUDA;
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0 && ms < best) best = ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    if (rc != SL_OK) return rc;
+    const double flops = 2.0 * blocks * threads * (double)kChains * kIters;
+    *gflops = flops / (best * 1e-3) / 1e9;
+    return SL_OK;
+}

@@ -1,0 +1,233 @@
+"""Parity of the GPU exact step with the oracle (which is pinned to the
+reference's own sim_one_step, tests/test_oracle_pin.py).
+
+Bar: positions, velocities, spins, acc and aacc bit-identical (the exact
+mode reproduces the reference's operation order and IEEE rounding);
+energy totals, which the GPU sums in another order, within rtol 1e-12.
+The headline tolerance of the hot path -- 1e-10 relative on positions and
+velocities after 100 steps at N=5000 -- is asserted too, as a floor."""
+import numpy as np
+import pytest
+
+from cases import GOLDEN_CASES, GOLDEN_CHECKPOINTS, OracleMaterial, contact_case, material, two_sphere_case
+from oracle.oracle import CpuOracle
+from spacelab_gb300 import BallGroup, GpuStep, SpaceLabError, configs
+from spacelab_gb300 import _lib
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = __import__("pathlib").Path(__file__).resolve().parent / "golden"
+STATE_KEYS = ("pos", "vel", "w", "acc", "aacc")
+E_RTOL = 1e-12
+
+
+def _gpu(c, mode="exact"):
+    g = BallGroup.from_arrays(c["pos"], c["vel"], c["w"], c["R"], c["m"], c["moi"])
+    s = GpuStep(g, material(), mode)
+    s.set_scalars(c["dt"], c["kin"], c["kout"])
+    return s
+
+
+def _oracle(c):
+    return CpuOracle(c["pos"], c["vel"], c["w"], c["R"], c["m"], c["moi"], OracleMaterial(), c["dt"], c["kin"],
+                     c["kout"])
+
+
+def _state(s):
+    g = s.download()
+    return {k: getattr(g, k).copy() for k in STATE_KEYS}
+
+
+def _assert_energy(e_gpu, e_ref):
+    e_gpu = e_gpu.as_array() if hasattr(e_gpu, "as_array") else np.asarray(e_gpu)
+    scale = np.maximum(np.abs(e_ref), 1e-300)
+    # mom/L components can cancel to ~0; compare against the magnitude scale
+    np.testing.assert_allclose(e_gpu[:2], e_ref[:2], rtol=E_RTOL, atol=0)
+    for sl in (slice(2, 5), slice(5, 8)):
+        mag = np.abs(e_ref[sl]).max() + 1e-300
+        assert np.abs(e_gpu[sl] - e_ref[sl]).max() <= 1e-12 * mag + 1e-300, (e_gpu[sl], e_ref[sl])
+
+
+@pytest.mark.parametrize("name", [c[0] for c in GOLDEN_CASES])
+def test_exact_matches_reference_golden(name):
+    g = np.load(GOLDEN / f"{name}.npz")
+    c = {k[3:]: g[k] for k in g.files if k.startswith("in_")}
+    for k in ("dt", "kin", "kout"):
+        c[k] = float(c[k])
+    s = _gpu(c)
+    e0 = s.init_conditions()
+    st = _state(s)
+    assert np.array_equal(st["acc"], g["init_acc"])
+    assert np.array_equal(st["aacc"], g["init_aacc"])
+    _assert_energy(e0, g["init_energy"])
+    assert np.array_equal(s.contacts(), g["contacts0"])
+    every = int(g["write_every"])
+    k = 0
+    for step in range(1, max(GOLDEN_CHECKPOINTS) + 1):
+        write = step % every == 0
+        e = s.sim_one_step(write)
+        if write:
+            _assert_energy(e, g["energies"][k])
+            k += 1
+        if step in GOLDEN_CHECKPOINTS:
+            st = _state(s)
+            for key in STATE_KEYS:
+                assert np.array_equal(st[key], g[f"step{step}_{key}"]), (name, step, key)
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 17, 31, 32, 33, 63, 64, 65, 100, 200])
+def test_exact_matches_oracle_ragged_sizes(n):
+    c = contact_case(n, 1000 + n)
+    s, o = _gpu(c), _oracle(c)
+    _assert_energy(s.init_conditions(), o.init())
+    assert np.array_equal(s.contacts(), o.contacts())
+    for step in range(1, 41):
+        write = step % 8 == 0
+        e = s.sim_one_step(write)
+        eo = o.step(write)
+        if write:
+            _assert_energy(e, eo)
+        if step % 10 == 0:
+            a, b = _state(s), o.state()
+            for key in STATE_KEYS:
+                assert np.array_equal(a[key], b[key]), (n, step, key)
+
+
+def test_two_spheres_touching_and_separated():
+    for gap in (-0.05, -1e-9, 0.0, 0.02, 5.0):
+        c = two_sphere_case(gap)
+        s, o = _gpu(c), _oracle(c)
+        _assert_energy(s.init_conditions(), o.init())
+        for step in range(1, 31):
+            s.sim_one_step(step % 5 == 0)
+            o.step(step % 5 == 0)
+        a, b = _state(s), o.state()
+        for key in STATE_KEYS:
+            assert np.array_equal(a[key], b[key]), (gap, key)
+
+
+def test_dense_contacts_n5000_step0_and_100_steps():
+    """Contact-rich N=5000 system: step-0 contact set identical, then 100
+    steps bit-identical to the oracle (row-parallel, all host cores)."""
+    c = contact_case(5000, 5000, vel_sigma=20.0)
+    s, o = _gpu(c), _oracle(c)
+    _assert_energy(s.init_conditions(), o.init())
+    cg, co = s.contacts(), o.contacts()
+    assert len(co) > 5000
+    assert np.array_equal(cg, co)
+    for step in range(1, 101):
+        write = step % 50 == 0
+        e = s.sim_one_step(write)
+        eo = o.step(write, threads=0)
+        if write:
+            np.testing.assert_allclose(e.KE, eo[1], rtol=E_RTOL)
+            np.testing.assert_allclose(e.PE, eo[0], rtol=1e-11)
+    a, b = _state(s), o.state()
+    for key in ("pos", "vel"):
+        rel = np.abs(a[key] - b[key]).max() / np.abs(b[key]).max()
+        assert rel <= 1e-10
+    for key in STATE_KEYS:
+        assert np.array_equal(a[key], b[key]), key
+
+
+def test_aggregate_collision_n5000_100_steps():
+    """The N=5000 benchmark workload: step-0 contact set, then 100 steps
+    within 1e-10 relative (and in fact bit-identical) to the oracle."""
+    w = configs.aggregate_collision_5000()
+    c = dict(pos=w.group.pos, vel=w.group.vel, w=w.group.w, R=w.group.R, m=w.group.m, moi=w.group.moi, dt=w.dt,
+             kin=w.kin, kout=w.kout)
+    s, o = _gpu(c), _oracle(c)
+    _assert_energy(s.init_conditions(), o.init())
+    assert np.array_equal(s.contacts(), o.contacts())
+    for step in range(1, 101):
+        write = step % w.skip == 0
+        e = s.sim_one_step(write)
+        eo = o.step(write, threads=0)
+        if write:
+            _assert_energy(e, eo)
+    a, b = _state(s), o.state()
+    for key in ("pos", "vel"):
+        assert np.abs(a[key] - b[key]).max() <= 1e-10 * np.abs(b[key]).max()
+    for key in STATE_KEYS:
+        assert np.array_equal(a[key], b[key]), key
+
+
+def test_looper_graph_matches_single_steps():
+    c = contact_case(300, 77)
+    a, b = _gpu(c), _gpu(c)
+    a.init_conditions(); b.init_conditions()
+    rows = a.sim_looper(steps=61, skip=10)
+    ebs = []
+    for step in range(1, 61):
+        e = b.sim_one_step(step % 10 == 0)
+        if e is not None:
+            ebs.append(e)
+    assert len(rows) == len(ebs) == 6
+    for r, e in zip(rows, ebs):
+        assert r.PE == e.PE and r.KE == e.KE
+    sa, sb = _state(a), _state(b)
+    for key in STATE_KEYS:
+        assert np.array_equal(sa[key], sb[key])
+
+
+def test_resume_matches_continuous_run():
+    c = contact_case(128, 31)
+    a = _gpu(c)
+    a.init_conditions()
+    for step in range(1, 21):
+        a.sim_one_step(False)
+    mid = _state(a)
+    o = _oracle(c)
+    o.init()
+    for step in range(1, 20):
+        o.step(False)
+    prev = o.state()["pos"]  # positions one step before `mid`
+    b = _gpu(c)
+    b.group.pos[:] = mid["pos"]; b.group.vel[:] = mid["vel"]; b.group.w[:] = mid["w"]
+    b.group.acc[:] = mid["acc"]; b.group.aacc[:] = mid["aacc"]
+    b.upload_resume(pos_prev=prev)
+    for step in range(21, 41):
+        a.sim_one_step(False)
+        b.sim_one_step(False)
+    sa, sb = _state(a), _state(b)
+    for key in STATE_KEYS:
+        assert np.array_equal(sa[key], sb[key]), key
+
+
+def test_reciprocal_division_is_ieee_exact():
+    lib = _lib.lib()
+    rng = np.random.default_rng(0)
+    n = 1 << 20
+    a = rng.normal(0, 1, n) * 10.0 ** rng.uniform(-20, 20, n)
+    b = 10.0 ** rng.uniform(-15, 15, n)
+    # divisors with all-ones / all-zero significands and near-midpoint cases
+    b[:4096] = np.nextafter(2.0 ** rng.integers(-40, 40, 4096), 0)
+    b[4096:8192] = 2.0 ** rng.integers(-40, 40, 4096) * (1 + 2.0 ** -52)
+    a[8192:12288] = b[8192:12288] * (1 + rng.integers(1, 1 << 20, 4096) * 2.0 ** -53)
+    qr, qi = np.zeros(n), np.zeros(n)
+    assert lib.sl_diag_division(n, _lib.dptr(a), _lib.dptr(b), _lib.dptr(qr), _lib.dptr(qi)) == 0
+    assert np.array_equal(qi, a / b)  # the GPU's IEEE division agrees with numpy
+    assert np.array_equal(qr.view(np.int64), qi.view(np.int64))
+
+
+def test_nonfinite_state_is_reported_not_trapped():
+    c = contact_case(40, 3)
+    s = _gpu(c)
+    s.init_conditions()
+    s.set_scalars(1e300, c["kin"], c["kout"])
+    with pytest.raises(SpaceLabError) as ei:
+        s.step(3, write_last=True)
+    assert ei.value.code == _lib.SL_ERR_NONFINITE
+
+
+def test_bad_inputs_rejected():
+    c = contact_case(10, 4)
+    c["R"] = c["R"].copy()
+    c["R"][3] = 0.0
+    with pytest.raises(SpaceLabError):
+        _gpu(c)
+    c = contact_case(10, 4)
+    c["pos"] = c["pos"].copy()
+    c["pos"][2, 1] = np.nan
+    with pytest.raises(SpaceLabError):
+        _gpu(c)
