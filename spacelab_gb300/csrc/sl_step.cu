@@ -257,20 +257,40 @@ __global__ void __launch_bounds__(128, 2) pair_tile_kernel(const __grid_constant
 // ------------------------------------------------- row sums + pass 3 ------
 // Thread (c, i): acc_c[i] = sum over partners j ascending of pairbuf[c][i][j]
 // (j != i), aacc_c[i] likewise over the contact partners, then pass 3.
-__global__ void __launch_bounds__(128) rowsum_kernel(const __grid_constant__ System s)
+// The sum is a dependent chain per (c, i), so the kernel is latency-bound:
+// each thread keeps kRowBatch 16-byte loads of its row in flight (register
+// double buffering) while it adds the previous batch.
+constexpr int kRowBatch = 16;
+constexpr int kRowThreads = 32;
+
+__global__ void __launch_bounds__(kRowThreads) rowsum_kernel(const __grid_constant__ System s)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 3 * s.n) return;
     const int c = t / s.n;
     const int i = t - c * s.n;
-    const size_t plane = (size_t)s.npad * s.npad;
-    const double* row = s.pairbuf + c * plane + (size_t)i * s.npad;
-    double acc = 0.0;
     const int n = s.n;
-    for (int j = 0; j < n; j += 2) {
-        const double2 v = __ldcs(reinterpret_cast<const double2*>(row + j));
-        if (j != i) acc += v.x;
-        if (j + 1 != i && j + 1 < n) acc += v.y;
+    const size_t plane = (size_t)s.npad * s.npad;
+    const double2* row = reinterpret_cast<const double2*>(s.pairbuf + c * plane + (size_t)i * s.npad);
+    const int nv = (n + 1) / 2;  // double2 words covering columns [0, n)
+    double2 cur[kRowBatch], nxt[kRowBatch];
+#pragma unroll
+    for (int k = 0; k < kRowBatch; ++k) cur[k] = k < nv ? __ldcs(row + k) : make_double2(0.0, 0.0);
+    double acc = 0.0;
+    for (int base = 0; base < nv; base += kRowBatch) {
+#pragma unroll
+        for (int k = 0; k < kRowBatch; ++k) {
+            const int q = base + kRowBatch + k;
+            nxt[k] = q < nv ? __ldcs(row + q) : make_double2(0.0, 0.0);
+        }
+#pragma unroll
+        for (int k = 0; k < kRowBatch; ++k) {
+            const int j = 2 * (base + k);
+            if (j < n && j != i) acc += cur[k].x;
+            if (j + 1 < n && j + 1 != i) acc += cur[k].y;
+        }
+#pragma unroll
+        for (int k = 0; k < kRowBatch; ++k) cur[k] = nxt[k];
     }
     double aacc = 0.0;
     const uint32_t* mrow = s.cmask + (size_t)i * s.nb;
@@ -386,7 +406,7 @@ void launch_step(const System& s, bool write, int num_sms, cudaStream_t st, Step
     else
         pair_tile_kernel<false><<<pb, 128, 0, st>>>(s);
     if (tm) cudaEventRecord(tm->ev[1], st);
-    rowsum_kernel<<<(3 * s.n + 127) / 128, 128, 0, st>>>(s);
+    rowsum_kernel<<<(3 * s.n + kRowThreads - 1) / kRowThreads, kRowThreads, 0, st>>>(s);
     if (tm) cudaEventRecord(tm->ev[2], st);
     if (write) {
         const int nred = kRedBlocks;

@@ -2,8 +2,13 @@
 reference's own sim_one_step, tests/test_oracle_pin.py).
 
 Bar: positions, velocities, spins, acc and aacc bit-identical (the exact
-mode reproduces the reference's operation order and IEEE rounding);
-energy totals, which the GPU sums in another order, within rtol 1e-12.
+mode reproduces the reference's operation order and IEEE rounding).
+Energy totals are sums the GPU forms in another order (a reduction tree
+instead of the reference's running sum), so they are compared against the
+magnitude of their terms: |dKE| <= 1e-12 KE; each momentum and angular-
+momentum component within 1e-12 x sum_i |term_i| (the totals themselves
+cancel to ~0 for a system at rest); PE (10^7 mixed-sign pair terms, and the
+GPU's log) within 1e-10 relative.
 The headline tolerance of the hot path -- 1e-10 relative on positions and
 velocities after 100 steps at N=5000 -- is asserted too, as a floor."""
 import numpy as np
@@ -19,6 +24,7 @@ pytestmark = pytest.mark.gpu
 GOLDEN = __import__("pathlib").Path(__file__).resolve().parent / "golden"
 STATE_KEYS = ("pos", "vel", "w", "acc", "aacc")
 E_RTOL = 1e-12
+PE_RTOL = 1e-10
 
 
 def _gpu(c, mode="exact"):
@@ -38,14 +44,25 @@ def _state(s):
     return {k: getattr(g, k).copy() for k in STATE_KEYS}
 
 
-def _assert_energy(e_gpu, e_ref):
+def _term_scales(st, m, moi):
+    """sum_i |m v_i|, sum_i |m (r x v)_i + moi w_i| per component."""
+    pos, vel, w = st["pos"], st["vel"], st["w"]
+    mom = (m[:, None] * np.abs(vel)).sum(0)
+    L = (m[:, None] * np.abs(np.cross(pos, vel)) + moi[:, None] * np.abs(w)).sum(0)
+    return mom, L
+
+
+def _assert_energy(e_gpu, e_ref, st=None, m=None, moi=None):
     e_gpu = e_gpu.as_array() if hasattr(e_gpu, "as_array") else np.asarray(e_gpu)
-    scale = np.maximum(np.abs(e_ref), 1e-300)
-    # mom/L components can cancel to ~0; compare against the magnitude scale
-    np.testing.assert_allclose(e_gpu[:2], e_ref[:2], rtol=E_RTOL, atol=0)
-    for sl in (slice(2, 5), slice(5, 8)):
-        mag = np.abs(e_ref[sl]).max() + 1e-300
-        assert np.abs(e_gpu[sl] - e_ref[sl]).max() <= 1e-12 * mag + 1e-300, (e_gpu[sl], e_ref[sl])
+    np.testing.assert_allclose(e_gpu[1], e_ref[1], rtol=E_RTOL, atol=0)
+    np.testing.assert_allclose(e_gpu[0], e_ref[0], rtol=PE_RTOL, atol=0)
+    if st is None:
+        scale_mom = np.abs(e_ref[2:5]).max() * np.ones(3)
+        scale_L = np.abs(e_ref[5:8]).max() * np.ones(3)
+    else:
+        scale_mom, scale_L = _term_scales(st, m, moi)
+    assert np.all(np.abs(e_gpu[2:5] - e_ref[2:5]) <= 1e-12 * scale_mom + 1e-300), (e_gpu[2:5], e_ref[2:5])
+    assert np.all(np.abs(e_gpu[5:8] - e_ref[5:8]) <= 1e-12 * scale_L + 1e-300), (e_gpu[5:8], e_ref[5:8])
 
 
 @pytest.mark.parametrize("name", [c[0] for c in GOLDEN_CASES])
@@ -79,14 +96,15 @@ def test_exact_matches_reference_golden(name):
 def test_exact_matches_oracle_ragged_sizes(n):
     c = contact_case(n, 1000 + n)
     s, o = _gpu(c), _oracle(c)
-    _assert_energy(s.init_conditions(), o.init())
+    e0 = o.init()
+    _assert_energy(s.init_conditions(), e0, o.state(), c["m"], c["moi"])
     assert np.array_equal(s.contacts(), o.contacts())
     for step in range(1, 41):
         write = step % 8 == 0
         e = s.sim_one_step(write)
         eo = o.step(write)
         if write:
-            _assert_energy(e, eo)
+            _assert_energy(e, eo, o.state(), c["m"], c["moi"])
         if step % 10 == 0:
             a, b = _state(s), o.state()
             for key in STATE_KEYS:
@@ -111,7 +129,8 @@ def test_dense_contacts_n5000_step0_and_100_steps():
     steps bit-identical to the oracle (row-parallel, all host cores)."""
     c = contact_case(5000, 5000, vel_sigma=20.0)
     s, o = _gpu(c), _oracle(c)
-    _assert_energy(s.init_conditions(), o.init())
+    e0 = o.init()
+    _assert_energy(s.init_conditions(), e0, o.state(), c["m"], c["moi"])
     cg, co = s.contacts(), o.contacts()
     assert len(co) > 5000
     assert np.array_equal(cg, co)
@@ -120,8 +139,7 @@ def test_dense_contacts_n5000_step0_and_100_steps():
         e = s.sim_one_step(write)
         eo = o.step(write, threads=0)
         if write:
-            np.testing.assert_allclose(e.KE, eo[1], rtol=E_RTOL)
-            np.testing.assert_allclose(e.PE, eo[0], rtol=1e-11)
+            _assert_energy(e, eo, o.state(), c["m"], c["moi"])
     a, b = _state(s), o.state()
     for key in ("pos", "vel"):
         rel = np.abs(a[key] - b[key]).max() / np.abs(b[key]).max()
@@ -137,14 +155,15 @@ def test_aggregate_collision_n5000_100_steps():
     c = dict(pos=w.group.pos, vel=w.group.vel, w=w.group.w, R=w.group.R, m=w.group.m, moi=w.group.moi, dt=w.dt,
              kin=w.kin, kout=w.kout)
     s, o = _gpu(c), _oracle(c)
-    _assert_energy(s.init_conditions(), o.init())
+    e0 = o.init()
+    _assert_energy(s.init_conditions(), e0, o.state(), c["m"], c["moi"])
     assert np.array_equal(s.contacts(), o.contacts())
     for step in range(1, 101):
         write = step % w.skip == 0
         e = s.sim_one_step(write)
         eo = o.step(write, threads=0)
         if write:
-            _assert_energy(e, eo)
+            _assert_energy(e, eo, o.state(), c["m"], c["moi"])
     a, b = _state(s), o.state()
     for key in ("pos", "vel"):
         assert np.abs(a[key] - b[key]).max() <= 1e-10 * np.abs(b[key]).max()
