@@ -147,6 +147,37 @@ int sl_kernel_times(sl_handle* h, double* pair_ms, double* rowsum_ms, long* laun
 /* Bytes of device memory the handle holds. */
 int sl_device_bytes(const sl_handle* h, uint64_t* bytes);
 
+/* Largest system sl_forces_static accepts. */
+#define SL_STATIC_MAX_SPHERES 256
+
+/* The initial force pass (what sl_init_forces computes) for a system that
+ * lives in the caller's own device memory, without allocating anything.
+ * No counterpart in the reference: it exists for callers that cannot call
+ * cudaMalloc -- code running inside a host application that owns and
+ * budgets all device memory and hands its plugins ready-made buffers, and
+ * code on a real-time path where an allocation's implicit device
+ * synchronisation and unbounded latency are not allowed.
+ *
+ * All pointers except mat are DEVICE pointers owned by the caller:
+ *   pos, vel, w      vec3[n] inputs (3n doubles each, x y z per sphere)
+ *   R, m, moi        double[n] inputs, each > 0
+ *   acc, aacc        vec3[n] outputs
+ *   energy           8 doubles out (PE, KE, mom xyz, ang_mom xyz), or NULL
+ * stream is a cudaStream_t (NULL = the legacy default stream); the call
+ * returns after the work on it has finished.  Initially touching pairs take
+ * k = kout, as in sl_init_forces.
+ *
+ * Limit: 1 <= n <= SL_STATIC_MAX_SPHERES; larger n returns SL_ERR_ARG.
+ * Working memory is one static device array of about 3.2 MB that every GPU
+ * loading this library holds until the process exits.  The first call on a
+ * device looks up that array's device address (cudaGetSymbolAddress), so make
+ * the first call on each device before any stream capture.  All calls share
+ * the array: calls whose work overlaps on the GPU (other host threads, or
+ * other streams) race and must be serialised by the caller. */
+int sl_forces_static(int n, const double* pos, const double* vel, const double* w, const double* R,
+                     const double* m, const double* moi, const sl_material* mat, double kin, double kout,
+                     double* acc, double* aacc, double* energy, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -71,6 +71,8 @@ _PROTOS = [
     ("sl_kernel_times", ctypes.c_int, [ctypes.c_void_p, _c_double_p, _c_double_p, ctypes.POINTER(ctypes.c_long),
                                        ctypes.c_int]),
     ("sl_device_bytes", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]),
+    ("sl_forces_static", ctypes.c_int, [ctypes.c_int] + [ctypes.c_void_p] * 6 + [ctypes.POINTER(Material),
+                                        ctypes.c_double, ctypes.c_double] + [ctypes.c_void_p] * 4),
     # diagnostics (spacelab_diag.h)
     ("sl_diag_division", ctypes.c_int, [ctypes.c_int] + [_c_double_p] * 4),
     ("sl_diag_fp64_peak", ctypes.c_int, [_c_double_p]),

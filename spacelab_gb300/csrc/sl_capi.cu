@@ -44,6 +44,13 @@ constexpr int kTimerPool = 8192;
 
 }  // namespace
 
+// Records `msg` as this thread's sl_last_error() text; used by entry points
+// in other translation units of the library.
+int sl_record_error(int code, const char* msg)
+{
+    return fail(code, msg ? std::string(msg) : std::string());
+}
+
 struct sl_handle {
     sl::System sys{};
     sl::Scalars host_sc{0, 0, 0};
