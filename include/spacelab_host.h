@@ -54,6 +54,37 @@ int slh_spring_and_dt(double r_max, double m_min, double speed, double rho, doub
  * reference's operation order (ball_group.hpp:519-547). */
 int slh_to_origin(int n, double* pos, const double* m);
 
+/* --- the reference's files (return 0, 1 bad argument, 3 I/O error, 4 format error) ---
+ * Writers produce the reference's formats: simData.csv (header
+ * ball_group.hpp:463-472; rows ColliderSingleCore.cpp:259,268-280),
+ * energy.csv (ball_group.hpp:462, ColliderSingleCore.cpp:335-338) and
+ * constants.csv (ball_group.hpp:475-477), numbers as printf("%.*g",
+ * precision): 6 is what the reference writes (lossy), 17 round-trips. */
+int slh_write_simdata_header(const char* path, int n);
+int slh_append_simdata_row(const char* path, int n, const double* pos, const double* w, const double* vel,
+                           int precision);
+int slh_write_energy_header(const char* path);
+int slh_append_energy_row(const char* path, double time, double PE, double KE, double p, double L, int precision);
+int slh_write_constants(const char* path, int n, const double* R, const double* m, const double* moi,
+                        int precision);
+/* Continue from a save (getLastLine/parseSimData/loadConsts,
+ * ball_group.hpp:979-1077): the state is the last row of simData.csv. */
+int slh_count_last_state(const char* simdata_path, int* n);
+int slh_read_last_state(const char* simdata_path, int n, double* pos, double* vel, double* w);
+int slh_read_constants(const char* constants_path, int n, double* R, double* m, double* moi);
+/* Exact binary checkpoint (no counterpart in the reference, whose CSV save
+ * keeps 6 digits and drops acc/aacc and the previous-step distances): the
+ * full state including previous positions, so that a resumed run
+ * (sl_upload_resume) continues bit for bit. */
+int slh_write_checkpoint(const char* path, int n, const double* pos, const double* vel, const double* w,
+                         const double* acc, const double* aacc, const double* pos_prev, const double* R,
+                         const double* m, const double* moi, double dt, double kin, double kout, double sim_time,
+                         long long step);
+int slh_read_checkpoint_header(const char* path, int* n, double* dt, double* kin, double* kout, double* sim_time,
+                               long long* step);
+int slh_read_checkpoint(const char* path, int n, double* pos, double* vel, double* w, double* acc, double* aacc,
+                        double* pos_prev, double* R, double* m, double* moi);
+
 /* Deterministic primitives, exported so tests can pin them. */
 double slh_log(double x);
 double slh_exp(double x);

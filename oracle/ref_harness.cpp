@@ -15,14 +15,31 @@
 //     save written at load time, because the reference constructs its global
 //     `Ball_group O(path, targetName, 0)` (ColliderSingleCore.cpp:33) from a
 //     saved simulation before main runs;
-//   * the reference's main() is renamed so the harness can export a C API.
+//   * the reference's main() is renamed so the harness can export a C API;
+//   * Ball_group's private members (its save loader) are made accessible to
+//     the harness by compiling the reference headers with `private` defined
+//     as `public`; every standard header the reference uses is included
+//     first, so only the reference's own classes see that definition.
+#include <algorithm>
+#include <array>
+#include <cassert>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
+#include <ctime>
 #include <fstream>
+#include <functional>
+#include <iomanip>
+#include <iosfwd>
 #include <iostream>
+#include <limits.h>
 #include <numbers>
+#include <random>
+#include <sstream>
 #include <string>
+#include <type_traits>
 #include <unistd.h>
 using std::isnan;
 
@@ -77,9 +94,11 @@ static std::string slref_dummy_dir()
 std::string path = slref_dummy_dir();
 std::string targetName = "slref_dummy_";
 
+#define private public
 #define main reference_main
 #include "ColliderSingleCore/ColliderSingleCore.cpp"
 #undef main
+#undef private
 
 static void slref_take_energy(double* e)
 {
@@ -148,6 +167,42 @@ void slref_get(double* pos, double* vel, double* w, double* acc, double* aacc)
             if (aacc) aacc[3 * i + c] = O.aacc[i][c];
         }
     }
+}
+
+// Load a save with the reference's own loader: Ball_group::loadSim =
+// getLastLine + parseSimData + loadConsts (ball_group.hpp:1236-1247).
+int slref_load_sim(const char* path, const char* name, int maxn, int* n, double* pos, double* vel, double* w,
+                   double* R, double* m, double* moi)
+{
+    Ball_group g;
+    g.loadSim(path, name);
+    *n = g.num_particles;
+    if (g.num_particles > maxn) return 1;
+    for (int i = 0; i < g.num_particles; i++) {
+        for (int c = 0; c < 3; c++) {
+            pos[3 * i + c] = g.pos[i][c];
+            vel[3 * i + c] = g.vel[i][c];
+            w[3 * i + c] = g.w[i][c];
+        }
+        R[i] = g.R[i]; m[i] = g.m[i]; moi[i] = g.moi[i];
+    }
+    return 0;
+}
+
+// Write a save with the reference's own writer, Ball_group::sim_init_write
+// (ball_group.hpp:421-516): simData header + one row, constants, energy.
+int slref_write_sim(const char* prefix, int n, const double* pos, const double* vel, const double* w,
+                    const double* R, const double* m, const double* moi)
+{
+    Ball_group g(n);
+    for (int i = 0; i < n; i++) {
+        g.pos[i] = vec3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+        g.vel[i] = vec3(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2]);
+        g.w[i] = vec3(w[3 * i], w[3 * i + 1], w[3 * i + 2]);
+        g.R[i] = R[i]; g.m[i] = m[i]; g.moi[i] = moi[i];
+    }
+    g.sim_init_write(prefix);
+    return 0;
 }
 
 }  // extern "C"

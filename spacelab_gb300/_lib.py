@@ -22,6 +22,7 @@ SL_ERR_STATE = 5
 SL_ERR_UNSUPPORTED = 6
 
 SL_MODE_EXACT = 0
+SL_MODE_MIXED = 1
 
 _c_double_p = ctypes.POINTER(ctypes.c_double)
 _c_int_p = ctypes.POINTER(ctypes.c_int)
@@ -85,6 +86,19 @@ _PROTOS = [
                                            ctypes.c_double, ctypes.c_uint64, ctypes.c_uint64] + [_c_double_p] * 6),
     ("slh_spring_and_dt", ctypes.c_int, [ctypes.c_double] * 6 + [_c_double_p] * 3),
     ("slh_to_origin", ctypes.c_int, [ctypes.c_int, _c_double_p, _c_double_p]),
+    ("slh_write_simdata_header", ctypes.c_int, [ctypes.c_char_p, ctypes.c_int]),
+    ("slh_append_simdata_row", ctypes.c_int, [ctypes.c_char_p, ctypes.c_int] + [_c_double_p] * 3 + [ctypes.c_int]),
+    ("slh_write_energy_header", ctypes.c_int, [ctypes.c_char_p]),
+    ("slh_append_energy_row", ctypes.c_int, [ctypes.c_char_p] + [ctypes.c_double] * 5 + [ctypes.c_int]),
+    ("slh_write_constants", ctypes.c_int, [ctypes.c_char_p, ctypes.c_int] + [_c_double_p] * 3 + [ctypes.c_int]),
+    ("slh_count_last_state", ctypes.c_int, [ctypes.c_char_p, _c_int_p]),
+    ("slh_read_last_state", ctypes.c_int, [ctypes.c_char_p, ctypes.c_int] + [_c_double_p] * 3),
+    ("slh_read_constants", ctypes.c_int, [ctypes.c_char_p, ctypes.c_int] + [_c_double_p] * 3),
+    ("slh_write_checkpoint", ctypes.c_int, [ctypes.c_char_p, ctypes.c_int] + [_c_double_p] * 9 +
+     [ctypes.c_double] * 4 + [ctypes.c_longlong]),
+    ("slh_read_checkpoint_header", ctypes.c_int, [ctypes.c_char_p, _c_int_p] + [_c_double_p] * 4 +
+     [ctypes.POINTER(ctypes.c_longlong)]),
+    ("slh_read_checkpoint", ctypes.c_int, [ctypes.c_char_p, ctypes.c_int] + [_c_double_p] * 9),
     ("slh_log", ctypes.c_double, [ctypes.c_double]),
     ("slh_exp", ctypes.c_double, [ctypes.c_double]),
     ("slh_rng_next", ctypes.c_uint64, [ctypes.POINTER(ctypes.c_uint64)]),
