@@ -32,6 +32,7 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "pair-interactions/s at N=5000 (FP64 aggregate collision)"
 UNIT = "pair-interactions/s"
+WORKLOADS = ("aggregate_collision_n5000", "dust_cluster_n1000", "polydisperse_cluster_n20000")
 
 
 def _dist_env():
@@ -39,16 +40,42 @@ def _dist_env():
         os.environ.get("LOCAL_RANK", "0"))
 
 
-def _workload():
+def replica_throughput(units_per_rank: float, ms_local: float, world: int, device: str = "cpu") -> tuple[float, float]:
+    """Whole-job throughput of `world` independent replicas: every rank did
+    `units_per_rank` units in `ms_local` ms; the job takes the slowest rank's
+    time.  Returns (units/s over all ranks, max ms).  Uses torch.distributed
+    when world > 1 (NCCL on GPUs, gloo on CPU)."""
+    ms_max = ms_local
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([ms_local], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_max = float(t.item())
+    return units_per_rank * world / (ms_max * 1e-3), ms_max
+
+
+def _workload(name: str = "aggregate_collision_n5000"):
     from spacelab_gb300 import configs
-    return configs.aggregate_collision_5000()
+    return {"aggregate_collision_n5000": configs.aggregate_collision_5000,
+            "dust_cluster_n1000": configs.dust_cluster_1000,
+            "polydisperse_cluster_n20000": configs.polydisperse_cluster_20000}[name]()
+
+
+def _metric(w, mode: str) -> str:
+    if w.name == "aggregate_collision_n5000" and mode == "exact":
+        return METRIC
+    return f"pair-interactions/s at N={w.n} ({'FP64' if mode == 'exact' else 'mixed FP32/FP64'} {w.name})"
 
 
 def _config(w, extra=None):
-    cfg = {"workload": w.name, "n_spheres": w.n, "n_target": 4000, "n_projectile": 1000, "steps_per_write": w.skip,
+    npad = (w.n + 31) // 32 * 32
+    cfg = {"workload": w.name, "n_spheres": w.n, "steps_per_write": w.skip,
            "dt_s": w.dt, "kin": w.kin, "kout": w.kout, "seeds": w.info,
-           "l2": "per-step working set > L2: the pair-term buffer (3*npad^2 doubles, 606 MB) is streamed "
-                 "through HBM every step"}
+           "l2": f"per-step working set > L2: the pair-term buffer (3*npad^2 terms, "
+                 f"{3 * npad * npad * 8 / 1e6:.0f} MB as FP64) is streamed through HBM every step"}
+    if w.name == "aggregate_collision_n5000":
+        cfg.update({"n_target": 4000, "n_projectile": 1000})
     if extra:
         cfg.update(extra)
     return cfg
@@ -158,9 +185,9 @@ def run_ours(args, rank, world, local_rank) -> dict | None:
     from spacelab_gb300 import GpuStep, _lib
     from spacelab_gb300 import flops as F
 
-    w = _workload()
+    w = _workload(args.workload)
     g = w.group
-    sim = GpuStep(g.copy(), w.material, "exact")
+    sim = GpuStep(g.copy(), w.material, args.mode)
     sim.set_scalars(w.dt, w.kin, w.kout)
     sim.init_conditions()
     stream = torch.cuda.ExternalStream(sim.stream_ptr())
@@ -187,29 +214,27 @@ def run_ours(args, rank, world, local_rank) -> dict | None:
     barrier()
     clk = clocks.stop()
     ms = ev0.elapsed_time(ev1)
-    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    ms_max = float(t.item())
-    pairs = w.pairs_per_step * args.steps * world
-    value = pairs / (ms_max * 1e-3)
-    gpu_launches = 3 * args.steps + 2 * nwrites
+    value, ms_max = replica_throughput(w.pairs_per_step * args.steps, ms, world, device="cuda")
+    gpu_launches = sim.step_launches(False) * (args.steps - nwrites) + sim.step_launches(True) * nwrites
+    pair_launches = (sim.step_launches(False) - 1) // 2
 
-    # per-kernel timing of the pair kernel (non-write steps), same stream
+    # per-step timing of the pair pass (non-write steps), same stream: with
+    # the pipelined exact step the pair span holds all pair phases and the
+    # row sums that run beside them; "rowsum" is the exposed remainder
     sim.kernel_timing(True)
     nk = max(10, min(50, args.steps))
     sim.step(nk, write_last=False)
     pair_ms, rowsum_ms, launches = sim.kernel_times(reset=True)
     sim.kernel_timing(False)
     contacts = int(len(sim.contacts()))
-    pair_ms_avg = pair_ms / launches
+    pair_ms_avg = pair_ms / launches  # one record per step
     flops_launch = F.pair_flops(w.pairs_per_step, contacts, write=False)
     peak = _lib.lib()
     pk = __import__("ctypes").c_double()
     _lib.check(peak.sl_diag_fp64_peak(__import__("ctypes").byref(pk)), "sl_diag_fp64_peak")
     peak_tflops = pk.value / 1e3
     achieved_tflops = flops_launch / (pair_ms_avg * 1e-3) / 1e12
-    traffic = _read_profile_traffic()
+    traffic = _read_profile_traffic() if (args.mode == "exact" and w.name == "aggregate_collision_n5000") else None
 
     # end to end through the C ABI with host buffers (upload + step + download)
     e2e = run_e2e(sim, w, min(args.steps, 60))
@@ -220,19 +245,22 @@ def run_ours(args, rank, world, local_rank) -> dict | None:
     if rank != 0:
         return None
     res = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "metric": _metric(w, args.mode), "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded clusters; no dataset)",
-        "config": _config(w, {"parallelism": "replicas" if world > 1 else "single GPU", "mode": "exact"}),
+        "vs_baseline": None, "dtype": "f64" if args.mode == "exact" else "f32+f64",
+        "data": "synthetic (seeded clusters; no dataset)",
+        "config": _config(w, {"parallelism": "replicas" if world > 1 else "single GPU", "mode": args.mode}),
         "impl": "ours",
         "e2e": e2e,
         "gpu_launches": gpu_launches,
-        "roofline": {"bound": "fp64", "kernel": "pair_tile_kernel", "achieved": achieved_tflops,
+        "roofline": {"bound": "fp64", "kernel": "pair_tile_kernel" if args.mode == "exact" else "mixed_pair_kernel",
+                     "achieved": achieved_tflops,
                      "peak": peak_tflops, "unit": "TFLOP/s", "frac": achieved_tflops / peak_tflops,
                      "traffic": traffic,
                      "peak_source": "measured live: FP64 FMA chains (sl_diag_fp64_peak), 2 flops per FMA",
-                     "flops_per_launch": flops_launch, "pair_ms_per_launch": pair_ms_avg,
-                     "rowsum_ms_per_launch": rowsum_ms / launches,
+                     "flops_per_step": flops_launch, "pair_ms_per_step": pair_ms_avg,
+                     "rowsum_exposed_ms_per_step": rowsum_ms / launches,
+                     "pair_launches_per_step": pair_launches,
                      "flop_convention": "add/sub/mul/div/sqrt = 1 flop each (spacelab_gb300/flops.py); "
                                         "div and sqrt cost ~7.5 FMA on this GPU",
                      "contacts": contacts},
@@ -281,12 +309,128 @@ def run_e2e(sim, w, steps: int) -> dict:
             "api": "sl_upload_resume + sl_step(1) + sl_download per step"}
 
 
+# --------------------------------------------------- mixed vs FP64 report --
+def run_drift(args) -> dict:
+    """Mixed-precision form against the FP64 form on the same seed: energy
+    drift |E(t) - E(0)| / |E(0)| of each, their difference, the final
+    position and velocity error, and both throughputs."""
+    import torch
+    from spacelab_gb300 import GpuStep
+    w = _workload(args.workload)
+    out = {"metric": f"mixed vs FP64 on {w.name}", "workload": w.name, "n_spheres": w.n, "steps": args.drift_steps,
+           "steps_per_write": w.skip}
+    runs = {}
+    for mode in ("exact", "mixed"):
+        sim = GpuStep(w.group.copy(), w.material, mode)
+        sim.set_scalars(w.dt, w.kin, w.kout)
+        e0 = sim.init_conditions()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rows = sim.sim_looper(steps=args.drift_steps + 1, skip=w.skip)
+        el = time.perf_counter() - t0
+        g = sim.download()
+        runs[mode] = {"E0": e0.PE + e0.KE, "E": np.array([r.E for r in rows]), "pos": g.pos.copy(),
+                      "vel": g.vel.copy(), "pairs_per_s": w.pairs_per_step * args.drift_steps / el}
+        sim.close()
+    ex, mx = runs["exact"], runs["mixed"]
+    E0 = abs(ex["E0"])
+    out.update({
+        "energy_drift_fp64": float(np.abs(ex["E"] - ex["E0"]).max() / E0),
+        "energy_drift_mixed": float(np.abs(mx["E"] - mx["E0"]).max() / E0),
+        "energy_mixed_minus_fp64": float(np.abs(mx["E"] - ex["E"]).max() / E0),
+        "pos_err_rel_to_size": float(np.abs(mx["pos"] - ex["pos"]).max() / np.abs(ex["pos"]).max()),
+        "pos_err_rel_to_radius": float(np.abs(mx["pos"] - ex["pos"]).max() / float(w.group.R.max())),
+        "vel_err_rel_to_max": float(np.abs(mx["vel"] - ex["vel"]).max() / np.abs(ex["vel"]).max()),
+        "pairs_per_s_fp64": ex["pairs_per_s"], "pairs_per_s_mixed": mx["pairs_per_s"],
+        "speedup_mixed_over_fp64": mx["pairs_per_s"] / ex["pairs_per_s"],
+    })
+    return out
+
+
+# ------------------------------------------------------ batched collisions --
+def run_batched(args) -> dict:
+    """Collisions/s of the batched solver (one persistent launch over the
+    whole sweep, autotuned shape) next to the same kind of collisions run
+    one at a time through the single-system step."""
+    import torch
+    from spacelab_gb300 import batch as B
+    torch.cuda.init()
+    t0 = time.perf_counter()
+    cols = B.sample_collisions(args.batched, seed=3, nt_range=(args.nt_min, args.nt_max))
+    build_s = time.perf_counter() - t0
+    steps = args.batch_steps
+    run = B.BatchRun(cols, args.mode, steps=steps, skip=100)
+    tuned = run.autotune(sample_steps=2)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record()
+    wall = run.run(1, steps, do_init=True)
+    ev1.record()
+    torch.cuda.synchronize()
+    bad = int(run.status().sum())
+    counts = np.array([c.n for c in cols])
+    pair_evals = float((counts.astype(np.float64) * (counts - 1) / 2).sum()) * steps
+    k = min(len(cols), args.baseline_instances)
+    base_s, _ = B.run_per_instance(cols[:k], steps, 100, args.mode)
+    base_rate = k / base_s
+    step_s = B.run_per_instance_steps(cols[:k], steps, 100, args.mode)
+    step_rate = k / step_s
+    rate = len(cols) / wall
+    return {"metric": f"batched collisions/s ({len(cols)} collisions, {steps} steps each, {args.mode})",
+            "value": rate, "unit": "collisions/s", "higher_is_better": True, "impl": "ours",
+            "collisions": len(cols), "steps_per_collision": steps, "spheres_total": int(counts.sum()),
+            "spheres_per_collision": [int(counts.min()), int(counts.max())],
+            "wall_s": wall, "pair_interactions_per_s": pair_evals / wall, "nonfinite_instances": bad,
+            "autotune": tuned,
+            "per_instance_baseline": {"collisions": k, "seconds": base_s, "collisions_per_s": base_rate,
+                                      "how": "sl_run per instance (graph per write interval)"},
+            "per_step_launch_baseline": {"collisions": k, "seconds": step_s, "collisions_per_s": step_rate,
+                                         "how": "sl_step(1) per step per instance (sim_one_step drop-in)"},
+            "speedup_over_per_instance": rate / base_rate, "speedup_over_per_step_launches": rate / step_rate,
+            "build_s": build_s,
+            "dtype": "f64" if args.mode == "exact" else "f32+f64",
+            "data": "synthetic (seeded collision sweep; no dataset)"}
+
+
+# -------------------------------------------------------- surrogate study --
+def run_surrogate_study(args) -> dict:
+    """Train the 5-member BF16 MLP ensemble on collisions simulated by the
+    batched solver, screen a parameter sweep, re-run uncertain points plus a
+    random audit with the FP64 method, and account the cost."""
+    import torch
+    from spacelab_gb300 import batch as B
+    from spacelab_gb300 import surrogate as S
+    from spacelab_gb300 import sweep as W
+    torch.cuda.init()
+    steps = args.study_steps
+    t0 = time.perf_counter()
+    train = B.sample_collisions(args.train_collisions, seed=21, nt_range=W.NT_RANGE, clearance=W.CLEARANCE,
+                                k_speed_div=W.K_SPEED_DIV)
+    build_s = time.perf_counter() - t0
+    y, sim_info = W.simulate(train, steps, mode="mixed")
+    x = W.features(train)
+    ens = S.Ensemble(8, 4, members=5, seed=3)
+    fit = ens.fit(x, y, epochs=args.epochs, batch=256, lr=1e-3)
+    points = W.sample_params(args.sweep_points, seed=22)
+    res = W.screen_sweep(ens, points, steps, threshold=args.threshold, audit=args.audit, seed=23, sim_mode="exact",
+                         max_uncertain=args.max_uncertain)
+    mean_pred = np.abs(y.mean(0) - y).mean(0)  # the method without the network: predict the training mean
+    return {"metric": "surrogate-screened sweep cost ratio (full FP64 simulation / screened)",
+            "value": res["cost_ratio"], "unit": "x", "higher_is_better": True,
+            "train_collisions": len(train), "steps_per_collision": steps, "train_sim_s": sim_info["seconds"],
+            "train_sim_pairs_per_s": sim_info["pair_evals"] / sim_info["seconds"], "build_s": build_s,
+            "fit_s": fit["seconds"], "final_loss": fit["final_loss"], "outcomes": list(S.OUTCOMES),
+            "outcome_mean_abs_dev": mean_pred.tolist(), "screen": res,
+            "recipe": {"nt_range": list(W.NT_RANGE), "clearance_radii": W.CLEARANCE, "k_speed_div": W.K_SPEED_DIV},
+            "data": "synthetic (seeded collision sweep; no dataset)"}
+
+
 # ------------------------------------------------------------- reference --
 def run_reference(args, rank, world) -> dict | None:
     if rank != 0:
         return None
     from oracle.oracle import ref_available
-    w = _workload()
+    w = _workload(args.workload)
     t0 = time.perf_counter()
     if ref_available():
         # the reference's own sim_one_step (single-threaded by construction)
@@ -311,6 +455,27 @@ def main(argv=None) -> int:
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU oracle timing (rank 0)")
+    ap.add_argument("--mode", choices=["exact", "mixed"], default="exact")
+    ap.add_argument("--workload", choices=WORKLOADS, default="aggregate_collision_n5000")
+    ap.add_argument("--drift-steps", type=int, default=0,
+                    help="instead of the benchmark: run the mixed and the FP64 form side by side for this many "
+                         "steps and report energy drift and trajectory error")
+    ap.add_argument("--batched", type=int, default=0,
+                    help="instead of the benchmark: this many sampled collisions through the batched solver")
+    ap.add_argument("--batch-steps", type=int, default=300)
+    ap.add_argument("--baseline-instances", type=int, default=16)
+    ap.add_argument("--surrogate-study", action="store_true",
+                    help="instead of the benchmark: train the surrogate ensemble and screen a sweep")
+    ap.add_argument("--train-collisions", type=int, default=8000)
+    ap.add_argument("--sweep-points", type=int, default=100000)
+    ap.add_argument("--study-steps", type=int, default=4000)
+    ap.add_argument("--epochs", type=int, default=150)
+    ap.add_argument("--threshold", type=float, default=0.3)
+    ap.add_argument("--audit", type=float, default=0.01)
+    ap.add_argument("--max-uncertain", type=float, default=0.03,
+                    help="re-run at most this fraction of the sweep as uncertain (raises the threshold)")
+    ap.add_argument("--nt-min", type=int, default=64)
+    ap.add_argument("--nt-max", type=int, default=1600)
     args = ap.parse_args(argv)
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -320,10 +485,21 @@ def main(argv=None) -> int:
         if res is not None:
             print(json.dumps(res), flush=True)
         return 0
+    if args.drift_steps:
+        res = run_drift(args)
+        print(json.dumps(res), flush=True)
+        return 0
+    if args.batched:
+        res = run_batched(args)
+        print(json.dumps(res), flush=True)
+        return 0
+    if args.surrogate_study:
+        res = run_surrogate_study(args)
+        print(json.dumps(res), flush=True)
+        return 0
     res = run_ours(args, rank, world, local_rank)
     if res is not None:
-        sys.path.insert(0, str(ROOT / "tests"))
-        res["cpu_baseline"] = cpu_oracle_rate(_workload(), budget_s=args.cpu_budget, threads=0)
+        res["cpu_baseline"] = cpu_oracle_rate(_workload(args.workload), budget_s=args.cpu_budget, threads=0)
         print(json.dumps(res), flush=True)
     return 0
 

@@ -15,6 +15,12 @@ extern "C" {
  * q_ieee[i] = the IEEE double quotient a[i] / b[i].  Host arrays. */
 int sl_diag_division(int n, const double* a, const double* b, double* q_recip, double* q_ieee);
 
+/* For i < n, on the current GPU: out[i] = a[i]/b[i] and out[2n+i] =
+ * sqrt(|a[i]|) as the step kernels compute them (an FP64 estimate rounded
+ * exactly with integer arithmetic), out[n+i] and out[3n+i] = the hardware
+ * IEEE results.  Host arrays; out has 4n entries. */
+int sl_diag_exact_ops(int n, const double* a, const double* b, double* out);
+
 /* Measured FP64 fused-multiply-add throughput of the current GPU in
  * GFLOP/s (2 flops per FMA), from a kernel of independent FMA chains timed
  * with CUDA events. */

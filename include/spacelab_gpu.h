@@ -48,6 +48,9 @@ extern "C" {
 
 /* arithmetic modes of the pair step */
 #define SL_MODE_EXACT 0     /* FP64, reference operation order, bit-exact */
+#define SL_MODE_MIXED 1     /* FP32 pair forces/torques on FP64 displacements and
+                               squared gaps; FP64 positions, accumulation, energy
+                               sums; deterministic, not bit-exact */
 
 /* Material constants that the reference compiles in (dust_const.hpp:21-38):
  * G, Hamaker constant Ha, sliding and rolling friction u_s and u_r, and the
@@ -138,9 +141,23 @@ int sl_contacts(sl_handle* h, int* pairs, long max_pairs, long* count);
  * own work or timing events against the library's launches. */
 void* sl_stream(sl_handle* h);
 
+/* Exact mode pipelines each step: the pair tiles run in five block-column
+ * phases on the handle's stream, and the row sums over each phase's partner
+ * blocks run on a second stream while the later phases compute.  The sums
+ * keep their order, so results are bit-identical either way.  enable = 0
+ * runs one pair launch and then one row-sum launch.  Default: enabled.
+ * Mixed mode has no pipelined form (SL_ERR_UNSUPPORTED for enable != 0). */
+int sl_set_overlap(sl_handle* h, int enable);
+
+/* Kernel launches one step makes (a write step computes the energy too). */
+int sl_step_launches(const sl_handle* h, int write, int* count);
+
 /* Per-kernel timing: when enabled, every step records CUDA events around
  * the pair kernel and the row-sum kernel; sl_kernel_times returns their
- * accumulated milliseconds and launch counts since the last reset. */
+ * accumulated milliseconds and launch counts since the last reset.  With
+ * the pipelined step, "pair" spans all pair phases (the row sums of the
+ * earlier phases run inside it) and "row-sum" is the part of the row sums
+ * left after the last pair phase. */
 int sl_kernel_timing(sl_handle* h, int enable);
 int sl_kernel_times(sl_handle* h, double* pair_ms, double* rowsum_ms, long* launches, int reset);
 

@@ -85,6 +85,17 @@ int slh_read_checkpoint_header(const char* path, int* n, double* dt, double* kin
 int slh_read_checkpoint(const char* path, int n, double* pos, double* vel, double* w, double* acc, double* aacc,
                         double* pos_prev, double* R, double* m, double* moi);
 
+/* Outcome of a projectile-target collision from its final state (no
+ * counterpart in the reference, whose `bound` column is always 0,
+ * ball_group.hpp:496,502): connected components of spheres whose surface
+ * gap is below bond_gap; largest_fraction = mass of the heaviest component /
+ * total mass; stuck_fraction = projectile mass (spheres n_t..n-1) in it /
+ * projectile mass; rg = its radius of gyration; n_components = count. */
+int slh_collision_outcome(int n, int n_t, const double* pos, const double* R, const double* m, double bond_gap,
+                          double* largest_fraction, double* stuck_fraction, double* rg, int* n_components);
+/* Mass-weighted radius of gyration of a cluster. */
+int slh_radius_of_gyration(int n, const double* pos, const double* m, double* rg);
+
 /* Deterministic primitives, exported so tests can pin them. */
 double slh_log(double x);
 double slh_exp(double x);

@@ -68,15 +68,43 @@ _PROTOS = [
     ("sl_download", ctypes.c_int, [ctypes.c_void_p] + [_c_double_p] * 5),
     ("sl_contacts", ctypes.c_int, [ctypes.c_void_p, _c_int_p, ctypes.c_long, ctypes.POINTER(ctypes.c_long)]),
     ("sl_stream", ctypes.c_void_p, [ctypes.c_void_p]),
+    ("sl_set_overlap", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    ("sl_step_launches", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
     ("sl_kernel_timing", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     ("sl_kernel_times", ctypes.c_int, [ctypes.c_void_p, _c_double_p, _c_double_p, ctypes.POINTER(ctypes.c_long),
                                        ctypes.c_int]),
     ("sl_device_bytes", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]),
     ("sl_forces_static", ctypes.c_int, [ctypes.c_int] + [ctypes.c_void_p] * 6 + [ctypes.POINTER(Material),
                                         ctypes.c_double, ctypes.c_double] + [ctypes.c_void_p] * 4),
+    # batched solver (spacelab_batch.h)
+    ("sl_batch_create", ctypes.c_int, [ctypes.c_int, _c_int_p, ctypes.POINTER(Material), ctypes.c_int, ctypes.c_int,
+                                       ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
+    ("sl_batch_destroy", ctypes.c_int, [ctypes.c_void_p]),
+    ("sl_batch_upload", ctypes.c_int, [ctypes.c_void_p] + [_c_double_p] * 10),
+    ("sl_batch_set_shape", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
+    ("sl_batch_shape", ctypes.c_int, [ctypes.c_void_p, _c_int_p, _c_int_p, _c_int_p]),
+    ("sl_batch_autotune", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _c_int_p, _c_int_p, _c_double_p]),
+    ("sl_batch_run", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    ("sl_batch_download", ctypes.c_int, [ctypes.c_void_p] + [_c_double_p] * 5),
+    ("sl_batch_energy", ctypes.c_int, [ctypes.c_void_p, _c_double_p, _c_int_p]),
+    ("sl_batch_status", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint)]),
+    # surrogate network (spacelab_mlp.h)
+    ("sl_mlp_create", ctypes.c_int, [ctypes.c_int] * 5 + [ctypes.c_uint64, ctypes.POINTER(ctypes.c_void_p)]),
+    ("sl_mlp_destroy", ctypes.c_int, [ctypes.c_void_p]),
+    ("sl_mlp_num_params", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]),
+    ("sl_mlp_get_params", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float)]),
+    ("sl_mlp_set_params", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float)]),
+    ("sl_mlp_gradients", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
+                                        ctypes.c_int, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
+    ("sl_mlp_train", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
+                                    ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_uint64,
+                                    ctypes.POINTER(ctypes.c_float)]),
+    ("sl_mlp_predict", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float), ctypes.c_int,
+                                      ctypes.POINTER(ctypes.c_float)]),
     # diagnostics (spacelab_diag.h)
     ("sl_diag_division", ctypes.c_int, [ctypes.c_int] + [_c_double_p] * 4),
     ("sl_diag_fp64_peak", ctypes.c_int, [_c_double_p]),
+    ("sl_diag_exact_ops", ctypes.c_int, [ctypes.c_int] + [_c_double_p] * 3),
     # host setup (spacelab_host.h)
     ("slh_build_cluster", ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                          ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
@@ -99,6 +127,9 @@ _PROTOS = [
     ("slh_read_checkpoint_header", ctypes.c_int, [ctypes.c_char_p, _c_int_p] + [_c_double_p] * 4 +
      [ctypes.POINTER(ctypes.c_longlong)]),
     ("slh_read_checkpoint", ctypes.c_int, [ctypes.c_char_p, ctypes.c_int] + [_c_double_p] * 9),
+    ("slh_collision_outcome", ctypes.c_int, [ctypes.c_int, ctypes.c_int] + [_c_double_p] * 3 + [ctypes.c_double] +
+     [_c_double_p] * 3 + [_c_int_p]),
+    ("slh_radius_of_gyration", ctypes.c_int, [ctypes.c_int, _c_double_p, _c_double_p, _c_double_p]),
     ("slh_log", ctypes.c_double, [ctypes.c_double]),
     ("slh_exp", ctypes.c_double, [ctypes.c_double]),
     ("slh_rng_next", ctypes.c_uint64, [ctypes.POINTER(ctypes.c_uint64)]),

@@ -24,7 +24,7 @@ import numpy as np
 from . import _lib
 from ._lib import Energy, Material, SpaceLabError, check, dptr
 
-MODES = {"exact": _lib.SL_MODE_EXACT}
+MODES = {"exact": _lib.SL_MODE_EXACT, "mixed": _lib.SL_MODE_MIXED}
 
 
 class BallGroup:
@@ -217,6 +217,16 @@ class GpuStep:
 
     def stream_ptr(self) -> int:
         return int(self._lib.sl_stream(self._h) or 0)
+
+    def set_overlap(self, enable: bool) -> None:
+        """Exact mode: pipeline the row sums with the pair phases (default on)."""
+        check(self._lib.sl_set_overlap(self._h, int(enable)), "sl_set_overlap")
+
+    def step_launches(self, write: bool) -> int:
+        """Kernel launches of one step."""
+        c = ctypes.c_int()
+        check(self._lib.sl_step_launches(self._h, int(write), ctypes.byref(c)), "sl_step_launches")
+        return c.value
 
     def kernel_timing(self, enable: bool) -> None:
         check(self._lib.sl_kernel_timing(self._h, int(enable)), "sl_kernel_timing")

@@ -33,6 +33,10 @@ NVCC_COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ff
 NVCC_FILE_FLAGS = {
     "sl_step.cu": ["--fmad=false"],
     "sl_capi.cu": ["--fmad=false"],
+    "sl_static.cu": ["--fmad=false"],
+    "sl_batch.cu": ["--fmad=false"],
+    "sl_batch_capi.cu": ["--fmad=false"],
+    "sl_diag.cu": ["--fmad=false"],
 }
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-I", str(ROOT / "include")]
 

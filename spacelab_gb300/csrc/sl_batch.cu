@@ -1,0 +1,215 @@
+// sl_batch.cu -- batched exact FP64 solver: thousands of independent
+// systems (projectile-target collisions of uneven sphere counts) advanced by
+// ONE persistent launch.
+//
+// Each CTA takes whole instances from an atomic work queue (largest first)
+// and runs all of an instance's steps before taking the next one; the only
+// synchronisation is __syncthreads inside the CTA, so no CTA ever waits on
+// another.  Within an instance a step is the reference's three passes
+// (ColliderSingleCore.cpp:82-97, 100-256, 263-287):
+//   drift    one thread per sphere (strided);
+//   pairs    i-centric: thread i walks partners j ascending through j-tiles
+//            staged in shared memory and adds each term to its running sum
+//            in the order the reference adds them to acc[i] -- the result is
+//            bit-identical to the reference step, pair terms being computed
+//            in the reference's (A = max, B = min) orientation;
+//   kick     pass 3, plus the write-step energy totals reduced in a fixed
+//            tree inside the CTA.
+// The j-tile size (template) and threads per instance (block size) are
+// chosen by the host autotuner (sl_batch_capi.cu).
+#include "sl_batch.h"
+#include "sl_batch_common.cuh"
+#include "sl_fp64_exact.cuh"
+#include "sl_pair_exact.cuh"
+
+namespace sl {
+
+namespace {
+
+using batch::cta_sum8;
+using batch::drift;
+using batch::kick;
+
+template <int TILE>
+struct JTile {
+    double x[TILE], y[TILE], z[TILE], R[TILE], twoR[TILE], fourR[TILE], cR3[TILE];
+};
+
+// Pass 2 for one instance; returns this thread's share of the PE (pairs
+// are counted once, by the thread of sphere A).
+template <int TILE, bool WRITE>
+__device__ double pair_pass(const Batch& b, int off, int n, const Material& M, double kin, double kout,
+                            JTile<TILE>& jt)
+{
+    double pe = 0;
+    for (int ibase = 0; ibase < n; ibase += blockDim.x) {
+        const int i = ibase + threadIdx.x;
+        const bool active = i < n;
+        const int gi = off + (active ? i : 0);
+        const double xi = b.pos.c[0][gi], yi = b.pos.c[1][gi], zi = b.pos.c[2][gi];
+        const double Ri = b.R[gi], twoRi = b.twoR[gi], fourRi = b.fourR[gi], cR3i = b.cR3[gi];
+        const double mi = b.m[gi], imi = b.inv_m[gi], moii = b.moi[gi], imoii = b.inv_moi[gi];
+        double ax = 0, ay = 0, az = 0, tx = 0, ty = 0, tz = 0;
+        for (int jbase = 0; jbase < n; jbase += TILE) {
+            for (int t = threadIdx.x; t < TILE; t += blockDim.x) {
+                const int j = jbase + t;
+                if (j < n) {
+                    const int g = off + j;
+                    jt.x[t] = b.pos.c[0][g]; jt.y[t] = b.pos.c[1][g]; jt.z[t] = b.pos.c[2][g];
+                    jt.R[t] = b.R[g]; jt.twoR[t] = b.twoR[g]; jt.fourR[t] = b.fourR[g]; jt.cR3[t] = b.cR3[g];
+                }
+            }
+            __syncthreads();
+            if (active) {
+                const int jend = min(TILE, n - jbase);
+                for (int t = 0; t < jend; ++t) {
+                    const int j = jbase + t;
+                    if (j == i) continue;
+                    const bool iA = i > j;  // the reference's orientation: A = max, B = min
+                    const double Ax = iA ? xi : jt.x[t], Ay = iA ? yi : jt.y[t], Az = iA ? zi : jt.z[t];
+                    const double Bx = iA ? jt.x[t] : xi, By = iA ? jt.y[t] : yi, Bz = iA ? jt.z[t] : zi;
+                    const double RA = iA ? Ri : jt.R[t], RB = iA ? jt.R[t] : Ri;
+                    const double twoRA = iA ? twoRi : jt.twoR[t], twoRB = iA ? jt.twoR[t] : twoRi;
+                    const double fourRA = iA ? fourRi : jt.fourR[t], cR3A = iA ? cR3i : jt.cR3[t];
+                    const double sumRaRb = RA + RB;                                  // :104
+                    const double rx = Bx - Ax, ry = By - Ay, rz = Bz - Az;           // :105
+                    const double d2 = rx * rx + ry * ry + rz * rz;
+                    const double y = rsqrt_refined(d2);
+                    const double dist = sqrt_from_estimate(d2, d2 * y);              // :107
+                    const double overlap = sumRaRb - dist;                           // :110
+                    double fx, fy, fz;
+                    if (overlap > 0) {
+                        const int gA = off + (iA ? i : j), gB = off + (iA ? j : i);
+                        ContactIn in;
+                        for (int c = 0; c < 3; ++c) {
+                            in.prevA[c] = b.prev.c[c][gA]; in.prevB[c] = b.prev.c[c][gB];
+                            in.wA[c] = b.w.c[c][gA]; in.wB[c] = b.w.c[c][gB];
+                            in.vA[c] = b.vel.c[c][gA]; in.vB[c] = b.vel.c[c][gB];
+                        }
+                        in.mA = b.m[gA]; in.mB = b.m[gB]; in.kin = kin; in.kout = kout;
+                        const ContactOut o = contact_pair_exact<WRITE>(in, M, rx, ry, rz, dist, overlap, RA, RB,
+                                                                       twoRA, twoRB, fourRA, cR3A);
+                        fx = o.fx; fy = o.fy; fz = o.fz;
+                        const double qx = iA ? o.tax : o.tbx, qy = iA ? o.tay : o.tby, qz = iA ? o.taz : o.tbz;
+                        tx += div_by_recip(qx, moii, imoii);                         // :187-188
+                        ty += div_by_recip(qy, moii, imoii);
+                        tz += div_by_recip(qz, moii, imoii);
+                        if (WRITE && iA) pe += o.pe;
+                    } else {
+                        double h = fabs(overlap);                                    // :211-215
+                        if (h < M.h_min) h = M.h_min;
+                        const double coef = vdw_coef(h, RA, RB, twoRA, twoRB, fourRA, cR3A);
+                        fx = coef * div_from_estimate(rx, dist, rx * y);
+                        fy = coef * div_from_estimate(ry, dist, ry * y);
+                        fz = coef * div_from_estimate(rz, dist, rz * y);
+                        if (WRITE && iA) pe += vdw_energy(M.Ha, h, RA, RB, twoRA);
+                    }
+                    const double qx = div_from_estimate(fx, mi, fx * imi);           // :249-250
+                    const double qy = div_from_estimate(fy, mi, fy * imi);
+                    const double qz = div_from_estimate(fz, mi, fz * imi);
+                    if (iA) { ax += qx; ay += qy; az += qz; }
+                    else { ax -= qx; ay -= qy; az -= qz; }
+                }
+            }
+            __syncthreads();
+        }
+        if (active) {
+            b.acc.c[0][gi] = ax; b.acc.c[1][gi] = ay; b.acc.c[2][gi] = az;
+            b.aacc.c[0][gi] = tx; b.aacc.c[1][gi] = ty; b.aacc.c[2][gi] = tz;
+        }
+    }
+    return pe;
+}
+
+template <int TILE>
+__global__ void __launch_bounds__(256) batch_exact_kernel(const __grid_constant__ Batch b, int first_step, int nsteps,
+                                                          int skip, int do_init)
+{
+    __shared__ JTile<TILE> jt;
+    __shared__ double sh[8][32];
+    __shared__ int s_next;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_next = atomicAdd(b.counter, 1);
+        __syncthreads();
+        const int k = s_next;
+        if (k >= b.ninst) return;
+        const int inst = b.order[k];
+        const int off = b.off[inst], n = b.cnt[inst];
+        Material M = b.mat;
+        M.u_s = b.u_s[inst];
+        const double dt = b.dt[inst], kin = b.kin[inst], kout = b.kout[inst];
+        double* recs = b.energy + (size_t)inst * b.nrec * 8;
+        if (do_init) {  // initial forces: a step with dt = 0 (init_conditions)
+            drift(b, off, n, 0.0);
+            __syncthreads();
+            const double pe = pair_pass<TILE, true>(b, off, n, M, kin, kout, jt);
+            __syncthreads();
+            kick(b, inst, off, n, 0.0, true, pe, recs, sh);
+            __syncthreads();
+        }
+        for (int q = 0; q < nsteps; ++q) {
+            const int step = first_step + q;
+            const bool write = skip > 0 && step % skip == 0;
+            drift(b, off, n, dt);
+            __syncthreads();
+            double pe = 0;
+            if (write)
+                pe = pair_pass<TILE, true>(b, off, n, M, kin, kout, jt);
+            else
+                pair_pass<TILE, false>(b, off, n, M, kin, kout, jt);
+            __syncthreads();
+            const int r = write ? step / skip : 0;
+            kick(b, inst, off, n, dt, write, pe, recs + (size_t)(r < b.nrec ? r : b.nrec - 1) * 8, sh);
+            __syncthreads();
+        }
+    }
+}
+
+__global__ void batch_derive_kernel(const __grid_constant__ Batch b)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= b.total) return;
+    const double R = b.R[i], m = b.m[i], moi = b.moi[i];
+    b.twoR[i] = 2 * R;
+    b.fourR[i] = 4 * R;
+    b.cR3[i] = b.mat.Ha / 6 * 64 * R * R * R;
+    b.inv_m[i] = 1.0 / m;
+    b.inv_moi[i] = 1.0 / moi;
+    if (b.f_R) {
+        b.f_R[i] = d2f_bits(R, b.len_shift);
+        b.f_inv_m[i] = d2f_bits(1.0 / m, 0);
+        b.f_inv_moi[i] = d2f_bits(1.0 / moi, 0);
+    }
+}
+
+}  // namespace
+
+void launch_batch_derive(const Batch& b, cudaStream_t st)
+{
+    batch_derive_kernel<<<(b.total + 255) / 256, 256, 0, st>>>(b);
+}
+
+void launch_batch_exact(const Batch& b, int tile, int threads, int blocks, int first_step, int nsteps, int skip,
+                        int do_init, cudaStream_t st)
+{
+    switch (tile) {
+        case 32: batch_exact_kernel<32><<<blocks, threads, 0, st>>>(b, first_step, nsteps, skip, do_init); break;
+        case 64: batch_exact_kernel<64><<<blocks, threads, 0, st>>>(b, first_step, nsteps, skip, do_init); break;
+        default: batch_exact_kernel<128><<<blocks, threads, 0, st>>>(b, first_step, nsteps, skip, do_init); break;
+    }
+}
+
+int batch_max_blocks_per_sm(int tile, int threads, bool mixed)
+{
+    if (mixed) return batch_mixed_max_blocks_per_sm(tile, threads);
+    int nb = 0;
+    switch (tile) {
+        case 32: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_exact_kernel<32>, threads, 0); break;
+        case 64: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_exact_kernel<64>, threads, 0); break;
+        default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_exact_kernel<128>, threads, 0); break;
+    }
+    return nb;
+}
+
+}  // namespace sl

@@ -1,0 +1,45 @@
+// sl_batch.h -- device layout of a batch of independent systems (one
+// projectile-target collision each) advanced by one persistent launch.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "sl_device.cuh"
+
+namespace sl {
+
+// Energy record layout: [inst][rec][8] = PE, KE, mom xyz, ang_mom xyz.
+struct Batch {
+    int ninst;
+    int total;            // spheres over all instances
+    const int* order;     // instance processing order (largest first)
+    int* counter;         // work-queue head
+    const int* off;       // first sphere of each instance
+    const int* cnt;       // spheres of each instance
+    const double* dt;     // per-instance time step
+    const double* kin;    // per-instance spring constants
+    const double* kout;
+    const double* u_s;    // per-instance sliding friction
+    Vec3Soa pos, prev, vel, velh, w, wh, acc, aacc;
+    double *R, *m, *moi, *twoR, *fourR, *cR3, *inv_m, *inv_moi;
+    float *f_R, *f_inv_m, *f_inv_moi;  // mixed form (lengths scaled by 2^-len_shift)
+    int len_shift;
+    Material mat;         // G, Ha, u_r, h_min shared; u_s per instance
+    double* energy;       // [ninst][nrec][8]
+    int nrec;
+    unsigned* status;     // per instance: 1 = non-finite state
+};
+
+// Launch the persistent kernel over all instances: an initial force pass
+// when do_init, then steps first_step .. first_step+nsteps-1 with a write
+// (energy record) at every step divisible by skip.  Records: rec 0 = the
+// initial pass, rec k = after step k*skip.
+void launch_batch_exact(const Batch& b, int tile, int threads, int blocks, int first_step, int nsteps, int skip,
+                        int do_init, cudaStream_t st);
+void launch_batch_mixed(const Batch& b, int tile, int threads, int blocks, int first_step, int nsteps, int skip,
+                        int do_init, cudaStream_t st);
+void launch_batch_derive(const Batch& b, cudaStream_t st);
+int batch_max_blocks_per_sm(int tile, int threads, bool mixed);
+int batch_mixed_max_blocks_per_sm(int tile, int threads);
+
+}  // namespace sl

@@ -1,0 +1,354 @@
+// sl_batch_capi.cu -- extern "C" API of the batched solver
+// (include/spacelab_batch.h): a batch of independent systems in one device
+// arena, advanced by one persistent, graph-captured launch, with a
+// project-written autotuner for the j-tile size and threads per instance.
+#include "../../include/spacelab_batch.h"
+#include "../../include/spacelab_gpu.h"
+#include "sl_batch.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <numeric>
+#include <string>
+#include <vector>
+
+int sl_record_error(int code, const char* msg);
+
+namespace {
+
+#define SLB_CUDA(call)                                                                              \
+    do {                                                                                            \
+        cudaError_t e_ = (call);                                                                    \
+        if (e_ != cudaSuccess) return sl_record_error(SL_ERR_CUDA, (std::string(#call) + ": " +     \
+                                                                    cudaGetErrorString(e_)).c_str()); \
+    } while (0)
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+const int kTiles[3] = {32, 64, 128};
+const int kThreads[3] = {64, 128, 256};
+
+}  // namespace
+
+struct sl_batch {
+    sl::Batch b{};
+    int mode = SL_MODE_EXACT;
+    int steps = 0, skip = 0;
+    int num_sms = 0;
+    int tile = 64, threads = 128;
+    cudaStream_t stream = nullptr;
+    void* arena = nullptr;
+    size_t arena_bytes = 0;
+    double* snapshot = nullptr;  // initial state for the autotuner (device)
+    bool uploaded = false;
+    std::vector<int> counts, offsets;
+};
+
+namespace {
+
+int blocks_for(const sl_batch* h, int tile, int threads)
+{
+    int per_sm = sl::batch_max_blocks_per_sm(tile, threads, h->mode == SL_MODE_MIXED);
+    if (per_sm < 1) per_sm = 1;
+    long long blocks = (long long)per_sm * h->num_sms;
+    if (blocks > h->b.ninst) blocks = h->b.ninst;
+    return (int)blocks;
+}
+
+// One persistent launch over all instances, captured as a CUDA graph
+// (queue reset + kernel) and launched.
+int launch_run(sl_batch* h, int tile, int threads, int first_step, int nsteps, int do_init, int skip)
+{
+    const int blocks = blocks_for(h, tile, threads);
+    cudaGraph_t g;
+    SLB_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    cudaMemsetAsync(h->b.counter, 0, sizeof(int), h->stream);
+    if (h->mode == SL_MODE_MIXED)
+        sl::launch_batch_mixed(h->b, tile, threads, blocks, first_step, nsteps, skip, do_init, h->stream);
+    else
+        sl::launch_batch_exact(h->b, tile, threads, blocks, first_step, nsteps, skip, do_init, h->stream);
+    SLB_CUDA(cudaStreamEndCapture(h->stream, &g));
+    cudaGraphExec_t ge;
+    const cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return sl_record_error(SL_ERR_CUDA, cudaGetErrorString(e));
+    const cudaError_t e2 = cudaGraphLaunch(ge, h->stream);
+    const cudaError_t e3 = cudaStreamSynchronize(h->stream);
+    cudaGraphExecDestroy(ge);
+    if (e2 != cudaSuccess) return sl_record_error(SL_ERR_CUDA, cudaGetErrorString(e2));
+    if (e3 != cudaSuccess) return sl_record_error(SL_ERR_CUDA, cudaGetErrorString(e3));
+    return SL_OK;
+}
+
+// device-to-device copy of the 5 vec3 state arrays to/from the snapshot
+int snapshot_copy(sl_batch* h, bool save)
+{
+    const sl::Vec3Soa* v[5] = {&h->b.pos, &h->b.vel, &h->b.w, &h->b.acc, &h->b.aacc};
+    const size_t bytes = (size_t)h->b.total * sizeof(double);
+    for (int k = 0; k < 5; ++k)
+        for (int c = 0; c < 3; ++c) {
+            double* snap = h->snapshot + (size_t)(3 * k + c) * h->b.total;
+            if (save)
+                SLB_CUDA(cudaMemcpyAsync(snap, v[k]->c[c], bytes, cudaMemcpyDeviceToDevice, h->stream));
+            else
+                SLB_CUDA(cudaMemcpyAsync(v[k]->c[c], snap, bytes, cudaMemcpyDeviceToDevice, h->stream));
+        }
+    SLB_CUDA(cudaStreamSynchronize(h->stream));
+    return SL_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sl_batch_create(int ninst, const int* counts, const sl_material* mat, int mode, int steps, int skip,
+                    sl_batch** out)
+{
+    if (!out) return sl_record_error(SL_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    if (ninst < 1 || !counts || !mat) return sl_record_error(SL_ERR_ARG, "need ninst >= 1, counts and material");
+    if (mode != SL_MODE_EXACT && mode != SL_MODE_MIXED) return sl_record_error(SL_ERR_UNSUPPORTED, "unknown mode");
+    if (steps < 0 || skip < 1) return sl_record_error(SL_ERR_ARG, "need steps >= 0 and skip >= 1");
+    if (!(mat->h_min > 0)) return sl_record_error(SL_ERR_ARG, "h_min must be > 0");
+    long long total = 0;
+    for (int i = 0; i < ninst; ++i) {
+        if (counts[i] < 1) return sl_record_error(SL_ERR_ARG, "every instance needs >= 1 sphere");
+        total += counts[i];
+    }
+    if (total > (1ll << 30)) return sl_record_error(SL_ERR_ARG, "batch too large");
+    sl_batch* h = new (std::nothrow) sl_batch();
+    if (!h) return sl_record_error(SL_ERR_ALLOC, "host allocation failed");
+    h->mode = mode;
+    h->steps = steps;
+    h->skip = skip;
+    h->counts.assign(counts, counts + ninst);
+    h->offsets.resize(ninst);
+    std::exclusive_scan(h->counts.begin(), h->counts.end(), h->offsets.begin(), 0);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete h;
+        return sl_record_error(SL_ERR_CUDA, "cudaStreamCreate failed");
+    }
+    sl::Batch& b = h->b;
+    b.ninst = ninst;
+    b.total = (int)total;
+    b.nrec = steps / skip + 1;
+    b.mat = sl::Material{mat->G, mat->Ha, mat->u_s, mat->u_r, mat->h_min};
+    const size_t T = (size_t)total;
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off = align_up(off + bytes, 256); return o; };
+    size_t o_vec[8][3], o_sc[8], o_f[3];
+    for (auto& v : o_vec)
+        for (auto& c : v) c = take(T * sizeof(double));
+    for (auto& s : o_sc) s = take(T * sizeof(double));
+    for (auto& f : o_f) f = take(mode == SL_MODE_MIXED ? T * sizeof(float) : 0);
+    const size_t o_order = take(ninst * sizeof(int)), o_off = take(ninst * sizeof(int)),
+                 o_cnt = take(ninst * sizeof(int)), o_counter = take(sizeof(int));
+    const size_t o_par = take(4 * (size_t)ninst * sizeof(double));
+    const size_t o_en = take((size_t)ninst * b.nrec * 8 * sizeof(double));
+    const size_t o_st = take(ninst * sizeof(unsigned));
+    const size_t o_snap = take(15 * T * sizeof(double));
+    h->arena_bytes = off;
+    if (cudaMalloc(&h->arena, off) != cudaSuccess) {
+        sl_batch_destroy(h);
+        return sl_record_error(SL_ERR_ALLOC, "cudaMalloc of the batch arena failed");
+    }
+    char* base = static_cast<char*>(h->arena);
+    sl::Vec3Soa* vecs[8] = {&b.pos, &b.prev, &b.vel, &b.velh, &b.w, &b.wh, &b.acc, &b.aacc};
+    for (int v = 0; v < 8; ++v)
+        for (int c = 0; c < 3; ++c) vecs[v]->c[c] = reinterpret_cast<double*>(base + o_vec[v][c]);
+    double** scal[8] = {&b.R, &b.m, &b.moi, &b.twoR, &b.fourR, &b.cR3, &b.inv_m, &b.inv_moi};
+    for (int k = 0; k < 8; ++k) *scal[k] = reinterpret_cast<double*>(base + o_sc[k]);
+    if (mode == SL_MODE_MIXED) {
+        b.f_R = reinterpret_cast<float*>(base + o_f[0]);
+        b.f_inv_m = reinterpret_cast<float*>(base + o_f[1]);
+        b.f_inv_moi = reinterpret_cast<float*>(base + o_f[2]);
+    }
+    int* order = reinterpret_cast<int*>(base + o_order);
+    int* doff = reinterpret_cast<int*>(base + o_off);
+    int* dcnt = reinterpret_cast<int*>(base + o_cnt);
+    b.order = order; b.off = doff; b.cnt = dcnt;
+    b.counter = reinterpret_cast<int*>(base + o_counter);
+    double* par = reinterpret_cast<double*>(base + o_par);
+    b.dt = par; b.kin = par + ninst; b.kout = par + 2 * ninst; b.u_s = par + 3 * ninst;
+    b.energy = reinterpret_cast<double*>(base + o_en);
+    b.status = reinterpret_cast<unsigned*>(base + o_st);
+    h->snapshot = reinterpret_cast<double*>(base + o_snap);
+    // largest instances first: the work queue then balances like LPT scheduling
+    std::vector<int> ord(ninst);
+    std::iota(ord.begin(), ord.end(), 0);
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int c) { return counts[a] > counts[c]; });
+    cudaError_t e = cudaMemsetAsync(h->arena, 0, off, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(order, ord.data(), ninst * sizeof(int), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(doff, h->offsets.data(), ninst * sizeof(int), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dcnt, counts, ninst * sizeof(int), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) {
+        sl_batch_destroy(h);
+        return sl_record_error(SL_ERR_CUDA, cudaGetErrorString(e));
+    }
+    *out = h;
+    return SL_OK;
+}
+
+int sl_batch_destroy(sl_batch* h)
+{
+    if (!h) return SL_OK;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->arena) cudaFree(h->arena);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return SL_OK;
+}
+
+int sl_batch_upload(sl_batch* h, const double* pos, const double* vel, const double* w, const double* R,
+                    const double* m, const double* moi, const double* dt, const double* kin, const double* kout,
+                    const double* u_s)
+{
+    if (!h) return sl_record_error(SL_ERR_ARG, "null batch");
+    if (!pos || !vel || !w || !R || !m || !moi || !dt || !kin || !kout || !u_s)
+        return sl_record_error(SL_ERR_ARG, "NULL input array");
+    sl::Batch& b = h->b;
+    const size_t T = (size_t)b.total;
+    double rmax = 0;
+    for (size_t i = 0; i < T; ++i) {
+        if (!(R[i] > 0) || !(m[i] > 0) || !(moi[i] > 0)) return sl_record_error(SL_ERR_ARG, "R, m, moi must be > 0");
+        rmax = std::max(rmax, R[i]);
+    }
+    for (size_t i = 0; i < 3 * T; ++i)
+        if (!std::isfinite(pos[i]) || !std::isfinite(vel[i]) || !std::isfinite(w[i]))
+            return sl_record_error(SL_ERR_ARG, "non-finite position, velocity or spin");
+    for (int i = 0; i < b.ninst; ++i)
+        if (!(dt[i] >= 0) || !(kin[i] >= 0) || !(kout[i] >= 0) || !(u_s[i] >= 0))
+            return sl_record_error(SL_ERR_ARG, "per-instance dt, kin, kout, u_s must be >= 0");
+    int ex = 0;
+    std::frexp(rmax, &ex);
+    b.len_shift = ex - 1;
+    std::vector<double> tmp(T);
+    const double* v3[3] = {pos, vel, w};
+    sl::Vec3Soa* dv[3] = {&b.pos, &b.vel, &b.w};
+    for (int k = 0; k < 3; ++k)
+        for (int c = 0; c < 3; ++c) {
+            for (size_t i = 0; i < T; ++i) tmp[i] = v3[k][3 * i + c];
+            SLB_CUDA(cudaMemcpy(dv[k]->c[c], tmp.data(), T * sizeof(double), cudaMemcpyHostToDevice));
+        }
+    for (int c = 0; c < 3; ++c) {
+        SLB_CUDA(cudaMemset(b.acc.c[c], 0, T * sizeof(double)));
+        SLB_CUDA(cudaMemset(b.aacc.c[c], 0, T * sizeof(double)));
+    }
+    SLB_CUDA(cudaMemcpy(b.R, R, T * sizeof(double), cudaMemcpyHostToDevice));
+    SLB_CUDA(cudaMemcpy(b.m, m, T * sizeof(double), cudaMemcpyHostToDevice));
+    SLB_CUDA(cudaMemcpy(b.moi, moi, T * sizeof(double), cudaMemcpyHostToDevice));
+    const double* par[4] = {dt, kin, kout, u_s};
+    double* dpar = const_cast<double*>(b.dt);
+    for (int k = 0; k < 4; ++k)
+        SLB_CUDA(cudaMemcpy(dpar + (size_t)k * b.ninst, par[k], b.ninst * sizeof(double), cudaMemcpyHostToDevice));
+    SLB_CUDA(cudaMemset(b.status, 0, b.ninst * sizeof(unsigned)));
+    sl::launch_batch_derive(b, h->stream);
+    SLB_CUDA(cudaGetLastError());
+    SLB_CUDA(cudaStreamSynchronize(h->stream));
+    h->uploaded = true;
+    return SL_OK;
+}
+
+int sl_batch_set_shape(sl_batch* h, int tile, int threads)
+{
+    if (!h) return sl_record_error(SL_ERR_ARG, "null batch");
+    if ((tile != 32 && tile != 64 && tile != 128) || (threads != 64 && threads != 128 && threads != 256))
+        return sl_record_error(SL_ERR_ARG, "tile must be 32/64/128 and threads 64/128/256");
+    h->tile = tile;
+    h->threads = threads;
+    return SL_OK;
+}
+
+int sl_batch_autotune(sl_batch* h, int sample_steps, int* tile, int* threads, double* times_ms)
+{
+    if (!h || !h->uploaded) return sl_record_error(SL_ERR_STATE, "upload the batch first");
+    if (sample_steps < 1) return sl_record_error(SL_ERR_ARG, "sample_steps must be >= 1");
+    if (int r = snapshot_copy(h, true)) return r;
+    cudaEvent_t e0, e1;
+    SLB_CUDA(cudaEventCreate(&e0));
+    SLB_CUDA(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int bt = h->tile, bth = h->threads, k = 0;
+    for (int ti = 0; ti < 3; ++ti)
+        for (int hi = 0; hi < 3; ++hi, ++k) {
+            if (int r = snapshot_copy(h, false)) return r;
+            // first launch compiles nothing but warms the caches; time the second
+            if (int r = launch_run(h, kTiles[ti], kThreads[hi], 1, 1, 0, 0)) return r;
+            cudaEventRecord(e0, h->stream);
+            if (int r = launch_run(h, kTiles[ti], kThreads[hi], 2, sample_steps, 0, 0)) return r;
+            cudaEventRecord(e1, h->stream);
+            cudaEventSynchronize(e1);
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (times_ms) times_ms[k] = ms;
+            if (ms < best) { best = ms; bt = kTiles[ti]; bth = kThreads[hi]; }
+        }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (int r = snapshot_copy(h, false)) return r;
+    SLB_CUDA(cudaMemset(h->b.status, 0, h->b.ninst * sizeof(unsigned)));
+    h->tile = bt;
+    h->threads = bth;
+    if (tile) *tile = bt;
+    if (threads) *threads = bth;
+    return SL_OK;
+}
+
+int sl_batch_run(sl_batch* h, int first_step, int nsteps, int do_init)
+{
+    if (!h || !h->uploaded) return sl_record_error(SL_ERR_STATE, "upload the batch first");
+    if (first_step < 1 || nsteps < 0) return sl_record_error(SL_ERR_ARG, "need first_step >= 1, nsteps >= 0");
+    return launch_run(h, h->tile, h->threads, first_step, nsteps, do_init, h->skip);
+}
+
+int sl_batch_download(sl_batch* h, double* pos, double* vel, double* w, double* acc, double* aacc)
+{
+    if (!h) return sl_record_error(SL_ERR_ARG, "null batch");
+    const size_t T = (size_t)h->b.total;
+    std::vector<double> tmp(T);
+    double* outs[5] = {pos, vel, w, acc, aacc};
+    const sl::Vec3Soa* src[5] = {&h->b.pos, &h->b.vel, &h->b.w, &h->b.acc, &h->b.aacc};
+    for (int k = 0; k < 5; ++k) {
+        if (!outs[k]) continue;
+        for (int c = 0; c < 3; ++c) {
+            SLB_CUDA(cudaMemcpy(tmp.data(), src[k]->c[c], T * sizeof(double), cudaMemcpyDeviceToHost));
+            for (size_t i = 0; i < T; ++i) outs[k][3 * i + c] = tmp[i];
+        }
+    }
+    return SL_OK;
+}
+
+int sl_batch_energy(sl_batch* h, double* energy, int* nrec)
+{
+    if (!h) return sl_record_error(SL_ERR_ARG, "null batch");
+    if (nrec) *nrec = h->b.nrec;
+    if (energy)
+        SLB_CUDA(cudaMemcpy(energy, h->b.energy, (size_t)h->b.ninst * h->b.nrec * 8 * sizeof(double),
+                            cudaMemcpyDeviceToHost));
+    return SL_OK;
+}
+
+int sl_batch_status(sl_batch* h, unsigned* status)
+{
+    if (!h || !status) return sl_record_error(SL_ERR_ARG, "null argument");
+    SLB_CUDA(cudaMemcpy(status, h->b.status, h->b.ninst * sizeof(unsigned), cudaMemcpyDeviceToHost));
+    return SL_OK;
+}
+
+int sl_batch_shape(const sl_batch* h, int* tile, int* threads, int* blocks)
+{
+    if (!h) return sl_record_error(SL_ERR_ARG, "null batch");
+    if (tile) *tile = h->tile;
+    if (threads) *threads = h->threads;
+    if (blocks) *blocks = blocks_for(h, h->tile, h->threads);
+    return SL_OK;
+}
+
+}  // extern "C"

@@ -59,6 +59,10 @@ struct sl_handle {
     int device = 0;
     int num_sms = 0;
     cudaStream_t stream = nullptr;
+    // exact mode: side stream + events overlapping row sums with pair phases
+    sl::StepOverlap ov{};
+    bool has_ov = false;   // ov's stream and events exist
+    bool overlap = false;  // steps use them
     void* arena = nullptr;
     size_t arena_bytes = 0;
     double* staging = nullptr;  // pinned, 18 * npad doubles
@@ -85,6 +89,14 @@ int check_handle(const sl_handle* h)
     return SL_OK;
 }
 
+void launch_mode_step(sl_handle* h, bool write, sl::StepTimers* tm)
+{
+    if (h->mode == SL_MODE_MIXED)
+        sl::launch_step_mixed(h->sys, write, h->num_sms, h->stream, tm);
+    else
+        sl::launch_step(h->sys, write, h->num_sms, h->stream, tm, h->overlap ? &h->ov : nullptr);
+}
+
 // One step on the handle's stream, with optional timing events.
 int enqueue_step(sl_handle* h, bool write)
 {
@@ -98,7 +110,7 @@ int enqueue_step(sl_handle* h, bool write)
         }
         tm = &h->timers[h->timers_used++];
     }
-    sl::launch_step(h->sys, write, h->num_sms, h->stream, tm);
+    launch_mode_step(h, write, tm);
     SL_CUDA(cudaGetLastError());
     return SL_OK;
 }
@@ -172,7 +184,7 @@ int sl_create(int n, const sl_material* mat, int mode, sl_handle** out)
     if (n < 1) return fail(SL_ERR_ARG, "n must be >= 1");
     if (n > 46340) return fail(SL_ERR_ARG, "n > 46340 exceeds the reference's pair index range");
     if (!mat) return fail(SL_ERR_ARG, "material is NULL");
-    if (mode != SL_MODE_EXACT) return fail(SL_ERR_UNSUPPORTED, "unknown mode");
+    if (mode != SL_MODE_EXACT && mode != SL_MODE_MIXED) return fail(SL_ERR_UNSUPPORTED, "unknown mode");
     if (!(mat->h_min > 0)) return fail(SL_ERR_ARG, "h_min must be > 0");
 
     sl_handle* h = new (std::nothrow) sl_handle();
@@ -184,6 +196,15 @@ int sl_create(int n, const sl_material* mat, int mode, sl_handle** out)
     if (e != cudaSuccess) { delete h; return cuda_fail(e, "cudaDeviceGetAttribute"); }
     e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) { delete h; return cuda_fail(e, "cudaStreamCreate"); }
+    if (mode == SL_MODE_EXACT) {
+        h->has_ov = true;  // destroy releases whatever was created
+        e = cudaStreamCreateWithFlags(&h->ov.side, cudaStreamNonBlocking);
+        for (int p = 0; p < sl::kPairPhases && e == cudaSuccess; ++p)
+            e = cudaEventCreateWithFlags(&h->ov.phase[p], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ov.join, cudaEventDisableTiming);
+        if (e != cudaSuccess) { sl_destroy(h); return cuda_fail(e, "side stream / event creation"); }
+        h->overlap = true;
+    }
 
     sl::System& s = h->sys;
     s.n = n;
@@ -200,6 +221,9 @@ int sl_create(int n, const sl_material* mat, int mode, sl_handle** out)
         for (int c = 0; c < 3; ++c) o_vec[v][c] = take(np * sizeof(double));
     size_t o_sc[8];
     for (int k = 0; k < 8; ++k) o_sc[k] = take(np * sizeof(double));
+    size_t o_f[3] = {0, 0, 0};
+    if (mode == SL_MODE_MIXED)
+        for (int k = 0; k < 3; ++k) o_f[k] = take(np * sizeof(float));
     const size_t o_pair = take(3 * np * np * sizeof(double));
     const size_t o_torq = take(3 * np * np * sizeof(double));
     const size_t o_mask = take(np * s.nb * sizeof(uint32_t));
@@ -217,6 +241,11 @@ int sl_create(int n, const sl_material* mat, int mode, sl_handle** out)
         for (int c = 0; c < 3; ++c) vecs[v]->c[c] = reinterpret_cast<double*>(base + o_vec[v][c]);
     double** scal[8] = {&s.R, &s.m, &s.moi, &s.twoR, &s.fourR, &s.cR3, &s.inv_m, &s.inv_moi};
     for (int k = 0; k < 8; ++k) *scal[k] = reinterpret_cast<double*>(base + o_sc[k]);
+    if (mode == SL_MODE_MIXED) {
+        s.f_R = reinterpret_cast<float*>(base + o_f[0]);
+        s.f_inv_m = reinterpret_cast<float*>(base + o_f[1]);
+        s.f_inv_moi = reinterpret_cast<float*>(base + o_f[2]);
+    }
     s.pairbuf = reinterpret_cast<double*>(base + o_pair);
     s.torqbuf = reinterpret_cast<double*>(base + o_torq);
     s.cmask = reinterpret_cast<uint32_t*>(base + o_mask);
@@ -250,6 +279,12 @@ int sl_destroy(sl_handle* h)
     if (h->h_energy) cudaFreeHost(h->h_energy);
     if (h->h_status) cudaFreeHost(h->h_status);
     if (h->stream) cudaStreamDestroy(h->stream);
+    if (h->has_ov) {
+        if (h->ov.side) cudaStreamDestroy(h->ov.side);
+        for (int p = 0; p < sl::kPairPhases; ++p)
+            if (h->ov.phase[p]) cudaEventDestroy(h->ov.phase[p]);
+        if (h->ov.join) cudaEventDestroy(h->ov.join);
+    }
     delete h;
     return SL_OK;
 }
@@ -274,6 +309,12 @@ int sl_upload(sl_handle* h, const double* pos, const double* vel, const double* 
             return fail(SL_ERR_ARG, "R, m and moi must be finite and > 0 (sphere " + std::to_string(i) + ")");
     }
     if (int r = sl_upload_resume(h, pos, vel, w, nullptr, nullptr, nullptr)) return r;
+    // length scale of the mixed form: 2^len_shift within a factor 2 of max R
+    double rmax = 0;
+    for (int i = 0; i < n; ++i) rmax = R[i] > rmax ? R[i] : rmax;
+    int ex = 0;
+    std::frexp(rmax, &ex);
+    h->sys.len_shift = ex - 1;
     // padded spheres get R = m = moi = 1 (they are never paired)
     const double* src[3] = {R, m, moi};
     double* dst[3] = {h->sys.R, h->sys.m, h->sys.moi};
@@ -371,7 +412,7 @@ int sl_run(sl_handle* h, int first_step, int last_step, int skip, sl_energy* row
                 drop_graph(h);
                 cudaGraph_t g;
                 SL_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-                for (int k = 0; k < skip; ++k) sl::launch_step(h->sys, k == skip - 1, h->num_sms, h->stream, nullptr);
+                for (int k = 0; k < skip; ++k) launch_mode_step(h, k == skip - 1, nullptr);
                 SL_CUDA(cudaStreamEndCapture(h->stream, &g));
                 const cudaError_t e = cudaGraphInstantiate(&h->interval_exec, g, 0);
                 cudaGraphDestroy(g);
@@ -441,6 +482,29 @@ int sl_contacts(sl_handle* h, int* pairs, long max_pairs, long* count)
 }
 
 void* sl_stream(sl_handle* h) { return h ? static_cast<void*>(h->stream) : nullptr; }
+
+int sl_set_overlap(sl_handle* h, int enable)
+{
+    if (int r = check_handle(h)) return r;
+    if (enable && !h->has_ov) return fail(SL_ERR_UNSUPPORTED, "the pipelined step exists in exact mode only");
+    SL_CUDA(cudaStreamSynchronize(h->stream));
+    if (h->overlap != (enable != 0)) drop_graph(h);
+    h->overlap = enable != 0;
+    return SL_OK;
+}
+
+int sl_step_launches(const sl_handle* h, int write, int* count)
+{
+    if (int r = check_handle(h)) return r;
+    if (!count) return fail(SL_ERR_ARG, "count is NULL");
+    int np = 1;
+    if (h->mode == SL_MODE_EXACT && h->overlap) {
+        int cb[sl::kPairPhases + 1];
+        np = sl::phase_bounds(h->sys.nb, cb);
+    }
+    *count = 1 + 2 * np + (write ? 2 : 0);  // drift, pair + row-sum per phase, energy
+    return SL_OK;
+}
 
 int sl_kernel_timing(sl_handle* h, int enable)
 {

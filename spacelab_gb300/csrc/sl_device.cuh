@@ -51,7 +51,66 @@ struct System {
     unsigned int* status; // error bits (see SL_ERR_* in spacelab_gpu.h)
     const Scalars* sc;
     Material mat;
+    // mixed-precision form: per-sphere FP32 constants in lengths scaled by
+    // 2^-len_shift (a power of two near the largest radius); NULL otherwise
+    float *f_R, *f_inv_m, *f_inv_moi;
+    int len_shift;
 };
+
+// Operands of a pair's contact branch beyond positions and radii (the
+// contact branch is rare: O(N) of the O(N^2) pairs, so they are gathered
+// from global memory when needed).
+struct ContactIn {
+    double prevA[3], prevB[3];  // positions of the previous step
+    double wA[3], wB[3], vA[3], vB[3];
+    double mA, mB, kin, kout;
+};
+
+__device__ __forceinline__ ContactIn gather_contact(const System& s, int A, int B)
+{
+    ContactIn in;
+    for (int c = 0; c < 3; ++c) {
+        in.prevA[c] = s.prev.c[c][A]; in.prevB[c] = s.prev.c[c][B];
+        in.wA[c] = s.w.c[c][A]; in.wB[c] = s.w.c[c][B];
+        in.vA[c] = s.vel.c[c][A]; in.vB[c] = s.vel.c[c][B];
+    }
+    in.mA = s.m[A]; in.mB = s.m[B];
+    in.kin = s.sc->kin; in.kout = s.sc->kout;
+    return in;
+}
+
+// Exact float -> double (IEEE, bit manipulation on the integer pipe).
+// Float subnormals flush to a signed zero; Inf/NaN keep their class.
+__device__ __forceinline__ double f2d_bits(float f)
+{
+    const unsigned u = __float_as_uint(f);
+    const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
+    const unsigned e = (u >> 23) & 0xffu;
+    const unsigned long long m = u & 0x7fffffu;
+    if (e == 0) return __longlong_as_double((long long)sign);
+    const unsigned long long ed = (e == 0xffu) ? 0x7ffull : (unsigned long long)(e + 896u);
+    return __longlong_as_double((long long)(sign | (ed << 52) | (m << 29)));
+}
+
+// RN-even double -> float of x * 2^-shift (bit manipulation on the integer
+// pipe; an exact power-of-two scaling folded into the exponent).  Results
+// below the float normal range flush to a signed zero, above it give Inf.
+__device__ __forceinline__ float d2f_bits(double x, int shift)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned sign = (unsigned)(b >> 63) << 31;
+    const int e = (int)((b >> 52) & 0x7ffull);
+    if (e == 0) return __uint_as_float(sign);
+    const int fe = e - 1023 + 127 - shift;
+    if (fe <= 0) return __uint_as_float(sign);
+    if (fe >= 255 || e == 0x7ff) return __uint_as_float(sign | 0x7f800000u);
+    const unsigned long long mant = b & 0xfffffffffffffull;
+    const unsigned m23 = (unsigned)(mant >> 29);
+    const unsigned rem = (unsigned)(mant & 0x1fffffffull);
+    unsigned r = ((unsigned)fe << 23) | m23;
+    r += (rem > 0x10000000u || (rem == 0x10000000u && (m23 & 1u))) ? 1u : 0u;  // may carry into Inf
+    return __uint_as_float(sign | r);
+}
 
 // Correctly rounded quotient a / b given y = RN(1/b) (b > 0, normal range).
 // Two residual corrections after q0 = RN(a*y), following Markstein's

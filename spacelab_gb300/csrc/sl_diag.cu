@@ -2,6 +2,7 @@
 #include "../../include/spacelab_diag.h"
 #include "../../include/spacelab_gpu.h"
 #include "sl_device.cuh"
+#include "sl_fp64_exact.cuh"
 
 #include <cuda_runtime.h>
 
@@ -14,6 +15,22 @@ __global__ void division_kernel(int n, const double* a, const double* b, double*
     const double y = 1.0 / b[i];
     qr[i] = sl::div_by_recip(a[i], b[i], y);
     qi[i] = a[i] / b[i];
+}
+
+// out[0..n): quotient via estimate + integer rounding, [n..2n): hardware
+// quotient, [2n..3n): sqrt(|a|) via estimate, [3n..4n): hardware sqrt
+__global__ void exact_ops_kernel(int n, const double* a, const double* b, double* out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double x = a[i], y = b[i];
+    const double yi = sl::rsqrt_refined(y * y);  // ~1/|y|
+    out[i] = sl::div_from_estimate(x, y, x * (y < 0 ? -yi : yi));
+    out[n + i] = x / y;
+    const double ax = fabs(x);
+    const double r = sl::rsqrt_refined(ax);
+    out[2 * (size_t)n + i] = sl::sqrt_from_estimate(ax, ax * r);
+    out[3 * (size_t)n + i] = sqrt(ax);
 }
 
 constexpr int kChains = 8;
@@ -54,6 +71,26 @@ extern "C" int sl_diag_division(int n, const double* a, const double* b, double*
     }
     if (rc == SL_OK && (cudaMemcpy(q_recip, d + 2 * (size_t)n, bytes, cudaMemcpyDeviceToHost) != cudaSuccess ||
                         cudaMemcpy(q_ieee, d + 3 * (size_t)n, bytes, cudaMemcpyDeviceToHost) != cudaSuccess))
+        rc = SL_ERR_CUDA;
+    cudaFree(d);
+    return rc;
+}
+
+extern "C" int sl_diag_exact_ops(int n, const double* a, const double* b, double* out)
+{
+    if (n < 1 || !a || !b || !out) return SL_ERR_ARG;
+    double* d = nullptr;
+    const size_t bytes = (size_t)n * sizeof(double);
+    if (cudaMalloc(&d, 6 * bytes) != cudaSuccess) return SL_ERR_ALLOC;
+    int rc = SL_OK;
+    if (cudaMemcpy(d, a, bytes, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(d + n, b, bytes, cudaMemcpyHostToDevice) != cudaSuccess)
+        rc = SL_ERR_CUDA;
+    if (rc == SL_OK) {
+        exact_ops_kernel<<<(n + 255) / 256, 256>>>(n, d, d + n, d + 2 * (size_t)n);
+        if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) rc = SL_ERR_CUDA;
+    }
+    if (rc == SL_OK && cudaMemcpy(out, d + 2 * (size_t)n, 4 * bytes, cudaMemcpyDeviceToHost) != cudaSuccess)
         rc = SL_ERR_CUDA;
     cudaFree(d);
     return rc;

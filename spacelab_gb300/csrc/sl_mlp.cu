@@ -1,0 +1,498 @@
+// sl_mlp.cu -- the collision-outcome surrogate: an MLP (n_in -> H x L hidden
+// layers with GELU -> n_out) with BF16 weights and activations and FP32
+// accumulation, trained and evaluated on the GPU by this file's kernels
+// (include/spacelab_mlp.h).
+//
+// Every matrix product is one kernel, gemm_nt: C[M][N] = A[M][K] . B[N][K]^T
+// with A and B bf16 row-major (K contiguous), on the tensor cores through
+// mma.sync m16n8k16 (bf16 x bf16 -> f32) with ldmatrix-loaded fragments from
+// shared-memory tiles; the epilogue adds the bias and writes the FP32
+// pre-activation and/or the BF16 activation (GELU or identity).
+//   forward   Z_l = X_l W_l^T + b_l,  X_{l+1} = bf16(GELU(Z_l))
+//   backward  dW_l = dZ_l^T X_l   (A = dZ^T, B = X^T: transposed copies)
+//             dX_l = dZ_l W_l     (B = W^T: a transposed copy of W)
+//             dZ_{l-1} = bf16(dX_l * GELU'(Z_{l-1}))
+// Widths are padded to multiples of 32 with zero weights that stay zero
+// (their gradients are zero), so every GEMM dimension is tile-aligned.
+// FP32 master weights are updated with Adam; bf16 copies feed the GEMMs.
+#include "../../include/spacelab_mlp.h"
+#include "../../include/spacelab_gpu.h"
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <new>
+#include <random>
+#include <string>
+#include <vector>
+
+int sl_record_error(int code, const char* msg);
+
+namespace {
+
+using bf16 = __nv_bfloat16;
+
+constexpr int kTM = 64, kTN = 64, kTK = 32, kPadK = 8;  // CTA tile; smem row pad (bank spread)
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void ldsm_x4(uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3, const void* p)
+{
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"(smem_u32(p)));
+}
+
+__device__ __forceinline__ void ldsm_x2(uint32_t& r0, uint32_t& r1, const void* p)
+{
+    asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0,%1}, [%2];\n" : "=r"(r0), "=r"(r1) : "r"(smem_u32(p)));
+}
+
+__device__ __forceinline__ void mma_bf16(float* d, uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t b0,
+                                         uint32_t b1)
+{
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
+
+__device__ __forceinline__ float gelu_grad(float z)
+{
+    const float cdf = 0.5f * (1.0f + erff(z * 0.70710678118654752f));
+    const float pdf = 0.39894228040143268f * expf(-0.5f * z * z);
+    return cdf + z * pdf;
+}
+
+// C = A . B^T for bf16 A[M][K] (lda), B[N][K] (ldb); K % 32 == 0; any M, N.
+// act: 0 identity, 1 GELU (applied to the bf16 output only).
+__global__ void __launch_bounds__(128) gemm_nt_kernel(const bf16* __restrict__ A, int lda, const bf16* __restrict__ B,
+                                                      int ldb, const float* __restrict__ bias, float* Cf, bf16* Cb,
+                                                      int ldc, int M, int N, int K, int act)
+{
+    __shared__ __align__(16) bf16 As[kTM][kTK + kPadK];
+    __shared__ __align__(16) bf16 Bs[kTN][kTK + kPadK];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int m0 = blockIdx.y * kTM, n0 = blockIdx.x * kTN;
+    const int wm = (warp & 1) * 32, wn = (warp >> 1) * 32;
+    float acc[2][4][4] = {};
+    for (int k0 = 0; k0 < K; k0 += kTK) {
+        // 64 rows x 32 bf16 = 4 16-byte chunks per row; 128 threads x 2 chunks per matrix
+        for (int q = tid; q < kTM * 4; q += 128) {
+            const int r = q >> 2, c = (q & 3) * 8;
+            uint4 va = make_uint4(0, 0, 0, 0), vb = make_uint4(0, 0, 0, 0);
+            if (m0 + r < M) va = *reinterpret_cast<const uint4*>(A + (size_t)(m0 + r) * lda + k0 + c);
+            if (n0 + r < N) vb = *reinterpret_cast<const uint4*>(B + (size_t)(n0 + r) * ldb + k0 + c);
+            *reinterpret_cast<uint4*>(&As[r][c]) = va;
+            *reinterpret_cast<uint4*>(&Bs[r][c]) = vb;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < kTK; kk += 16) {
+            uint32_t a[2][4], b[4][2];
+#pragma unroll
+            for (int mt = 0; mt < 2; ++mt)
+                ldsm_x4(a[mt][0], a[mt][1], a[mt][2], a[mt][3], &As[wm + mt * 16 + (lane & 15)][kk + (lane >> 4) * 8]);
+#pragma unroll
+            for (int nt = 0; nt < 4; ++nt)
+                ldsm_x2(b[nt][0], b[nt][1], &Bs[wn + nt * 8 + (lane & 7)][kk + ((lane >> 3) & 1) * 8]);
+#pragma unroll
+            for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+                for (int nt = 0; nt < 4; ++nt)
+                    mma_bf16(acc[mt][nt], a[mt][0], a[mt][1], a[mt][2], a[mt][3], b[nt][0], b[nt][1]);
+        }
+        __syncthreads();
+    }
+    const int g = lane >> 2, t4 = lane & 3;
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int row = m0 + wm + mt * 16 + g + h * 8;
+                const int col = n0 + wn + nt * 8 + t4 * 2;
+                if (row >= M) continue;
+#pragma unroll
+                for (int e = 0; e < 2; ++e) {
+                    if (col + e >= N) continue;
+                    float v = acc[mt][nt][2 * h + e] + (bias ? bias[col + e] : 0.0f);
+                    if (Cf) Cf[(size_t)row * ldc + col + e] = v;
+                    if (Cb) Cb[(size_t)row * ldc + col + e] = __float2bfloat16(act ? gelu(v) : v);
+                }
+            }
+}
+
+// out[c][r] = in[r][c]
+__global__ void transpose_kernel(const bf16* __restrict__ in, int rows, int cols, int ldi, bf16* out, int ldo)
+{
+    __shared__ bf16 t[32][33];
+    const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
+    for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+        const int r = by + y, c = bx + threadIdx.x;
+        t[y][threadIdx.x] = (r < rows && c < cols) ? in[(size_t)r * ldi + c] : __float2bfloat16(0.0f);
+    }
+    __syncthreads();
+    for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+        const int c = bx + y, r = by + threadIdx.x;
+        if (c < cols && r < rows) out[(size_t)c * ldo + r] = t[threadIdx.x][y];
+    }
+}
+
+// float -> bf16 rows (input features, zero padding beyond n)
+__global__ void pack_input_kernel(const float* __restrict__ x, int M, int n, int ld, bf16* out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= M * ld) return;
+    const int r = i / ld, c = i - r * ld;
+    out[i] = __float2bfloat16(c < n ? x[(size_t)r * n + c] : 0.0f);
+}
+
+// MSE over the first n_out columns: dZ = 2 (z - y) / (M n_out), loss partials
+__global__ void mse_grad_kernel(const float* __restrict__ z, int ldz, const float* __restrict__ y, int M, int n_out,
+                                bf16* dz, int ld, float* loss_partial)
+{
+    __shared__ float red[256];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    float l = 0.0f;
+    if (i < M * ld) {
+        const int r = i / ld, c = i - r * ld;
+        float g = 0.0f;
+        if (c < n_out) {
+            const float e = z[(size_t)r * ldz + c] - y[(size_t)r * n_out + c];
+            l = e * e;
+            g = 2.0f * e / (float)(M * n_out);
+        }
+        dz[i] = __float2bfloat16(g);
+    }
+    red[threadIdx.x] = l;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) loss_partial[blockIdx.x] = red[0];
+}
+
+// dZ = bf16(dX * GELU'(Z)) elementwise
+__global__ void gelu_back_kernel(const float* __restrict__ dx, const float* __restrict__ z, int n, bf16* dz)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dz[i] = __float2bfloat16(dx[i] * gelu_grad(z[i]));
+}
+
+// db[c] = sum_r dZ[r][c]  (dZ bf16 [M][ld])
+__global__ void bias_grad_kernel(const bf16* __restrict__ dz, int M, int ld, int n, float* db)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    float s = 0.0f;
+    for (int r = 0; r < M; ++r) s += __bfloat162float(dz[(size_t)r * ld + c]);
+    db[c] = s;
+}
+
+// Adam on fp32 master parameters; refreshes the bf16 copy.  mask: the
+// parameter is live (padding stays 0).
+__global__ void adam_kernel(float* p, const float* g, float* m, float* v, bf16* pb, const uint8_t* mask, int n, float lr,
+                            float b1, float b2, float eps, float c1, float c2)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (mask && !mask[i]) return;
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.0f - b1) * gi;
+    const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    const float pi = p[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    p[i] = pi;
+    if (pb) pb[i] = __float2bfloat16(pi);
+}
+
+__global__ void to_bf16_kernel(const float* __restrict__ in, bf16* out, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = __float2bfloat16(in[i]);
+}
+
+int pad32(int x) { return (x + 31) / 32 * 32; }
+
+}  // namespace
+
+struct sl_mlp {
+    int n_in = 0, hidden = 0, layers = 0, n_out = 0, max_batch = 0;
+    int nl = 0;                          // linear layers = hidden layers + 1
+    std::vector<int> din, dout;          // padded widths of each linear layer
+    std::vector<size_t> w_off, b_off;    // offsets into the parameter vector
+    size_t nparam = 0;
+    float *P = nullptr, *G = nullptr, *Mom = nullptr, *Var = nullptr;  // fp32 params, grads, Adam moments
+    bf16* Pb = nullptr;                  // bf16 copy of params (weights used by the GEMMs)
+    uint8_t* mask = nullptr;             // live parameters
+    bf16 *Wt = nullptr;                  // transposed weights scratch (max din x dout)
+    std::vector<bf16*> X;                // bf16 activations per layer input [max_batch][din]
+    std::vector<float*> Z;               // fp32 pre-activations per layer [max_batch][dout]
+    bf16 *dZ = nullptr, *dZt = nullptr, *Xt = nullptr;
+    float* dX = nullptr;
+    float *xin = nullptr, *yin = nullptr, *loss_part = nullptr;
+    int step = 0;
+    void* arena = nullptr;
+};
+
+namespace {
+
+void gemm(cudaStream_t st, const bf16* A, int lda, const bf16* B, int ldb, const float* bias, float* Cf, bf16* Cb,
+          int ldc, int M, int N, int K, int act)
+{
+    dim3 grid((N + kTN - 1) / kTN, (M + kTM - 1) / kTM);
+    gemm_nt_kernel<<<grid, 128, 0, st>>>(A, lda, B, ldb, bias, Cf, Cb, ldc, M, N, K, act);
+}
+
+void transpose(cudaStream_t st, const bf16* in, int rows, int cols, int ldi, bf16* out, int ldo)
+{
+    dim3 grid((cols + 31) / 32, (rows + 31) / 32), block(32, 8);
+    transpose_kernel<<<grid, block, 0, st>>>(in, rows, cols, ldi, out, ldo);
+}
+
+// forward over M rows of xin (already on device); the output pre-activation
+// of the last layer is Z[nl-1] ([M][dout_last], fp32)
+void forward(sl_mlp* h, int M, cudaStream_t st)
+{
+    const int ld0 = h->din[0];
+    pack_input_kernel<<<(M * ld0 + 255) / 256, 256, 0, st>>>(h->xin, M, h->n_in, ld0, h->X[0]);
+    for (int l = 0; l < h->nl; ++l) {
+        const bool last = l == h->nl - 1;
+        gemm(st, h->X[l], h->din[l], h->Pb + h->w_off[l], h->din[l], h->P + h->b_off[l], h->Z[l],
+             last ? nullptr : h->X[l + 1], h->dout[l], M, h->dout[l], h->din[l], last ? 0 : 1);
+    }
+}
+
+// backward for M rows with targets yin; fills G
+void backward(sl_mlp* h, int M, cudaStream_t st)
+{
+    const int L = h->nl;
+    const int ldo = h->dout[L - 1];
+    const int nb = (M * ldo + 255) / 256;
+    mse_grad_kernel<<<nb, 256, 0, st>>>(h->Z[L - 1], ldo, h->yin, M, h->n_out, h->dZ, ldo, h->loss_part);
+    for (int l = L - 1; l >= 0; --l) {
+        const int K = h->din[l], N = h->dout[l];
+        // dW = dZ^T X : A = dZ^T [N][M], B = X^T [K][M]
+        transpose(st, h->dZ, M, N, N, h->dZt, M);
+        transpose(st, h->X[l], M, K, K, h->Xt, M);
+        gemm(st, h->dZt, M, h->Xt, M, nullptr, h->G + h->w_off[l], nullptr, K, N, K, M, 0);
+        bias_grad_kernel<<<(N + 127) / 128, 128, 0, st>>>(h->dZ, M, N, N, h->G + h->b_off[l]);
+        if (l == 0) break;
+        // dX = dZ W : A = dZ [M][N], B = W^T [K][N]
+        transpose(st, h->Pb + h->w_off[l], N, K, K, h->Wt, N);
+        gemm(st, h->dZ, N, h->Wt, N, nullptr, h->dX, nullptr, K, M, K, N, 0);
+        gelu_back_kernel<<<(M * K + 255) / 256, 256, 0, st>>>(h->dX, h->Z[l - 1], M * K, h->dZ);
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int sl_mlp_create(int n_in, int hidden, int hidden_layers, int n_out, int max_batch, uint64_t seed, sl_mlp** out)
+{
+    if (!out) return sl_record_error(SL_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    if (n_in < 1 || hidden < 1 || hidden_layers < 1 || n_out < 1 || max_batch < 32 || max_batch % 32)
+        return sl_record_error(SL_ERR_ARG, "need n_in, hidden, layers, n_out >= 1 and max_batch a multiple of 32");
+    sl_mlp* h = new (std::nothrow) sl_mlp();
+    if (!h) return sl_record_error(SL_ERR_ALLOC, "host allocation failed");
+    h->n_in = n_in; h->hidden = hidden; h->layers = hidden_layers; h->n_out = n_out; h->max_batch = max_batch;
+    h->nl = hidden_layers + 1;
+    for (int l = 0; l < h->nl; ++l) {
+        h->din.push_back(pad32(l == 0 ? n_in : hidden));
+        h->dout.push_back(pad32(l == h->nl - 1 ? n_out : hidden));
+    }
+    size_t off = 0;
+    for (int l = 0; l < h->nl; ++l) {
+        h->w_off.push_back(off); off += (size_t)h->din[l] * h->dout[l];
+        h->b_off.push_back(off); off += (size_t)h->dout[l];
+    }
+    h->nparam = off;
+    int maxw = 0;
+    for (int l = 0; l < h->nl; ++l) maxw = std::max(maxw, std::max(h->din[l], h->dout[l]));
+    // one arena
+    size_t bytes = 0;
+    auto take = [&](size_t b) { size_t o = bytes; bytes = (bytes + b + 255) / 256 * 256; return o; };
+    const size_t oP = take(off * 4), oG = take(off * 4), oM = take(off * 4), oV = take(off * 4), oPb = take(off * 2),
+                 oMask = take(off), oWt = take((size_t)maxw * maxw * 2);
+    std::vector<size_t> oX, oZ;
+    for (int l = 0; l < h->nl; ++l) {
+        oX.push_back(take((size_t)max_batch * h->din[l] * 2));
+        oZ.push_back(take((size_t)max_batch * h->dout[l] * 4));
+    }
+    const size_t odZ = take((size_t)max_batch * maxw * 2), odZt = take((size_t)max_batch * maxw * 2),
+                 oXt = take((size_t)max_batch * maxw * 2), odX = take((size_t)max_batch * maxw * 4),
+                 oxin = take((size_t)max_batch * n_in * 4), oyin = take((size_t)max_batch * n_out * 4),
+                 oloss = take(((size_t)max_batch * maxw / 256 + 1) * 4);
+    if (cudaMalloc(&h->arena, bytes) != cudaSuccess) {
+        delete h;
+        return sl_record_error(SL_ERR_ALLOC, "cudaMalloc of the MLP arena failed");
+    }
+    char* b = static_cast<char*>(h->arena);
+    h->P = (float*)(b + oP); h->G = (float*)(b + oG); h->Mom = (float*)(b + oM); h->Var = (float*)(b + oV);
+    h->Pb = (bf16*)(b + oPb); h->mask = (uint8_t*)(b + oMask); h->Wt = (bf16*)(b + oWt);
+    for (int l = 0; l < h->nl; ++l) { h->X.push_back((bf16*)(b + oX[l])); h->Z.push_back((float*)(b + oZ[l])); }
+    h->dZ = (bf16*)(b + odZ); h->dZt = (bf16*)(b + odZt); h->Xt = (bf16*)(b + oXt); h->dX = (float*)(b + odX);
+    h->xin = (float*)(b + oxin); h->yin = (float*)(b + oyin); h->loss_part = (float*)(b + oloss);
+    cudaMemset(h->arena, 0, bytes);
+    // He-style init of live weights, zero biases and padding
+    std::vector<float> p(off, 0.0f);
+    std::vector<uint8_t> mk(off, 0);
+    std::mt19937_64 rng(seed);
+    std::normal_distribution<float> nd(0.0f, 1.0f);
+    for (int l = 0; l < h->nl; ++l) {
+        const int kin = l == 0 ? n_in : hidden, nout = l == h->nl - 1 ? n_out : hidden;
+        const float sd = std::sqrt(2.0f / (float)kin);
+        for (int r = 0; r < nout; ++r)
+            for (int c = 0; c < kin; ++c) {
+                const size_t i = h->w_off[l] + (size_t)r * h->din[l] + c;
+                p[i] = sd * nd(rng);
+                mk[i] = 1;
+            }
+        for (int r = 0; r < nout; ++r) mk[h->b_off[l] + r] = 1;
+    }
+    cudaMemcpy(h->P, p.data(), off * 4, cudaMemcpyHostToDevice);
+    cudaMemcpy(h->mask, mk.data(), off, cudaMemcpyHostToDevice);
+    to_bf16_kernel<<<(int)((off + 255) / 256), 256>>>(h->P, h->Pb, (int)off);
+    if (cudaDeviceSynchronize() != cudaSuccess) {
+        sl_mlp_destroy(h);
+        return sl_record_error(SL_ERR_CUDA, "MLP initialisation failed");
+    }
+    *out = h;
+    return SL_OK;
+}
+
+int sl_mlp_destroy(sl_mlp* h)
+{
+    if (!h) return SL_OK;
+    if (h->arena) cudaFree(h->arena);
+    delete h;
+    return SL_OK;
+}
+
+int sl_mlp_num_params(const sl_mlp* h, int64_t* n)
+{
+    if (!h || !n) return sl_record_error(SL_ERR_ARG, "null argument");
+    *n = (int64_t)h->nparam;
+    return SL_OK;
+}
+
+int sl_mlp_get_params(sl_mlp* h, float* params)
+{
+    if (!h || !params) return sl_record_error(SL_ERR_ARG, "null argument");
+    if (cudaMemcpy(params, h->P, h->nparam * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return sl_record_error(SL_ERR_CUDA, "copy failed");
+    return SL_OK;
+}
+
+int sl_mlp_set_params(sl_mlp* h, const float* params)
+{
+    if (!h || !params) return sl_record_error(SL_ERR_ARG, "null argument");
+    if (cudaMemcpy(h->P, params, h->nparam * 4, cudaMemcpyHostToDevice) != cudaSuccess)
+        return sl_record_error(SL_ERR_CUDA, "copy failed");
+    to_bf16_kernel<<<(int)((h->nparam + 255) / 256), 256>>>(h->P, h->Pb, (int)h->nparam);
+    if (cudaDeviceSynchronize() != cudaSuccess) return sl_record_error(SL_ERR_CUDA, "bf16 refresh failed");
+    return SL_OK;
+}
+
+int sl_mlp_gradients(sl_mlp* h, const float* x, const float* y, int M, float* grads, float* loss)
+{
+    if (!h || !x || !y || M < 32 || M % 32 || M > h->max_batch)
+        return sl_record_error(SL_ERR_ARG, "M must be a multiple of 32 up to max_batch");
+    cudaMemcpy(h->xin, x, (size_t)M * h->n_in * 4, cudaMemcpyHostToDevice);
+    cudaMemcpy(h->yin, y, (size_t)M * h->n_out * 4, cudaMemcpyHostToDevice);
+    forward(h, M, nullptr);
+    backward(h, M, nullptr);
+    if (cudaDeviceSynchronize() != cudaSuccess) return sl_record_error(SL_ERR_CUDA, "MLP step failed");
+    if (grads) cudaMemcpy(grads, h->G, h->nparam * 4, cudaMemcpyDeviceToHost);
+    if (loss) {
+        const int ldo = h->dout[h->nl - 1];
+        const int nb = (M * ldo + 255) / 256;
+        std::vector<float> part(nb);
+        cudaMemcpy(part.data(), h->loss_part, nb * 4, cudaMemcpyDeviceToHost);
+        double s = 0;
+        for (float v : part) s += v;
+        *loss = (float)(s / ((double)M * h->n_out));
+    }
+    return SL_OK;
+}
+
+int sl_mlp_train(sl_mlp* h, const float* x, const float* y, int n, int epochs, int batch, float lr, uint64_t seed,
+                 float* loss_per_epoch)
+{
+    if (!h || !x || !y || n < batch || batch < 32 || batch % 32 || batch > h->max_batch || epochs < 1)
+        return sl_record_error(SL_ERR_ARG, "bad training arguments");
+    std::vector<int> idx(n);
+    for (int i = 0; i < n; ++i) idx[i] = i;
+    std::mt19937_64 rng(seed);
+    std::vector<float> xb((size_t)batch * h->n_in), yb((size_t)batch * h->n_out);
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    const int ldo = h->dout[h->nl - 1];
+    const int nb = (batch * ldo + 255) / 256;
+    std::vector<float> part(nb);
+    int rc = SL_OK;
+    for (int ep = 0; ep < epochs && rc == SL_OK; ++ep) {
+        std::shuffle(idx.begin(), idx.end(), rng);
+        double ls = 0;
+        int steps = 0;
+        for (int s0 = 0; s0 + batch <= n; s0 += batch) {
+            for (int r = 0; r < batch; ++r) {
+                std::memcpy(&xb[(size_t)r * h->n_in], &x[(size_t)idx[s0 + r] * h->n_in], h->n_in * 4);
+                std::memcpy(&yb[(size_t)r * h->n_out], &y[(size_t)idx[s0 + r] * h->n_out], h->n_out * 4);
+            }
+            cudaMemcpyAsync(h->xin, xb.data(), xb.size() * 4, cudaMemcpyHostToDevice, nullptr);
+            cudaMemcpyAsync(h->yin, yb.data(), yb.size() * 4, cudaMemcpyHostToDevice, nullptr);
+            forward(h, batch, nullptr);
+            backward(h, batch, nullptr);
+            ++h->step;
+            const float c1 = 1.0f - std::pow(b1, (float)h->step), c2 = 1.0f - std::pow(b2, (float)h->step);
+            adam_kernel<<<(int)((h->nparam + 255) / 256), 256>>>(h->P, h->G, h->Mom, h->Var, h->Pb, h->mask,
+                                                                 (int)h->nparam, lr, b1, b2, eps, c1, c2);
+            cudaMemcpy(part.data(), h->loss_part, nb * 4, cudaMemcpyDeviceToHost);
+            double s = 0;
+            for (float v : part) s += v;
+            ls += s / ((double)batch * h->n_out);
+            ++steps;
+        }
+        if (cudaGetLastError() != cudaSuccess) rc = sl_record_error(SL_ERR_CUDA, "training kernel failed");
+        if (loss_per_epoch) loss_per_epoch[ep] = (float)(ls / std::max(1, steps));
+    }
+    if (cudaDeviceSynchronize() != cudaSuccess && rc == SL_OK) rc = sl_record_error(SL_ERR_CUDA, "training failed");
+    return rc;
+}
+
+int sl_mlp_predict(sl_mlp* h, const float* x, int n, float* y)
+{
+    if (!h || !x || !y || n < 1) return sl_record_error(SL_ERR_ARG, "bad arguments");
+    const int B = h->max_batch, L = h->nl, ldo = h->dout[L - 1];
+    std::vector<float> zb((size_t)B * ldo);
+    for (int s0 = 0; s0 < n; s0 += B) {
+        const int M = std::min(B, n - s0);
+        const int Mp = (M + 31) / 32 * 32;
+        cudaMemset(h->xin, 0, (size_t)Mp * h->n_in * 4);
+        cudaMemcpy(h->xin, x + (size_t)s0 * h->n_in, (size_t)M * h->n_in * 4, cudaMemcpyHostToDevice);
+        forward(h, Mp, nullptr);
+        if (cudaMemcpy(zb.data(), h->Z[L - 1], (size_t)M * ldo * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+            return sl_record_error(SL_ERR_CUDA, "prediction failed");
+        for (int r = 0; r < M; ++r)
+            for (int c = 0; c < h->n_out; ++c) y[(size_t)(s0 + r) * h->n_out + c] = zb[(size_t)r * ldo + c];
+    }
+    return SL_OK;
+}
+
+}  // extern "C"

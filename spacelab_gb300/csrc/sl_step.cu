@@ -16,9 +16,14 @@
 //                     |L| (:282-285), in a fixed reduction tree.
 // All arithmetic follows the reference's vec3 evaluation order
 // (vec3.hpp:44-128,180-184) and this file is compiled with --fmad=false, so
-// no multiply-add is contracted; fma() appears only in div_by_recip.
+// no multiply-add is contracted.  The square root and the quotients of the
+// non-contact path and of the mass divisions are formed as FP64 estimates
+// rounded exactly with integer arithmetic (sl_fp64_exact.cuh): the same
+// IEEE results with most of the work moved off the narrow FP64 pipe.
 #include "sl_device.cuh"
 #include "sl_kernels.h"
+#include "sl_fp64_exact.cuh"
+#include "sl_pair_exact.cuh"
 
 #include <cstdio>
 
@@ -49,117 +54,27 @@ struct ABlock {
         m[kBlock], inv_m[kBlock];
 };
 
-// vdW force magnitude prefix chain of ColliderSingleCore.cpp:135-139 /
-// :221-225:  Ha/6*64*Ra*Ra*Ra*Rb*Rb*Rb * ((h+Ra+Rb) / (S*S*T*T)),
-// S = h2 + 2Ra h + 2Rb h, T = S + 4 Ra Rb; cR3 = ((Ha/6*64)*Ra)*Ra*Ra.
-__device__ __forceinline__ double vdw_coef(double h, double Ra, double Rb, double twoRa, double twoRb,
-                                           double fourRa, double cR3a)
-{
-    const double h2 = h * h;
-    const double S = h2 + twoRa * h + twoRb * h;
-    const double T = S + fourRa * Rb;
-    return cR3a * Rb * Rb * Rb * ((h + Ra + Rb) / (S * S * T * T));
-}
-
-// U_vdw of ColliderSingleCore.cpp:195-202 / :231-238.
-__device__ __forceinline__ double vdw_energy(double Ha, double h, double Ra, double Rb, double twoRa)
-{
-    const double sumRaRb = Ra + Rb;
-    const double diffRaRb = Ra - Rb;
-    const double z = sumRaRb + h;
-    const double two_RaRb = twoRa * Rb;
-    const double denom_sum = z * z - (sumRaRb * sumRaRb);
-    const double denom_diff = z * z - (diffRaRb * diffRaRb);
-    return -Ha / 6 * (two_RaRb / denom_sum + two_RaRb / denom_diff + log(denom_sum / denom_diff));
-}
-
-struct ContactOut {
-    double fx, fy, fz;      // totalForceOnA
-    double tax, tay, taz;   // torqueA
-    double tbx, tby, tbz;   // torqueB
-    double pe;
-};
-
-// Contact branch, ColliderSingleCore.cpp:119-204, for the pair (A, B),
-// A > B, rVecab = pos[B] - pos[A].  Rare (O(N) of the O(N^2) pairs), so its
-// operands beyond positions and radii are fetched here from global memory.
-template <bool WRITE>
-__device__ __noinline__ ContactOut contact_pair(const System& s, int A, int B, double rx, double ry,
-                                                double rz, double dist, double overlap, double Ra,
-                                                double Rb, double twoRa, double twoRb, double fourRa,
-                                                double cR3a)
-{
-    const Material& M = s.mat;
-    const double sumRaRb = Ra + Rb;
-    // k from the previous-step distance (:119-126), recomputed from the
-    // previous positions with the same operation sequence as `dist`.
-    const double px = s.prev.c[0][B] - s.prev.c[0][A];
-    const double py = s.prev.c[1][B] - s.prev.c[1][A];
-    const double pz = s.prev.c[2][B] - s.prev.c[2][A];
-    const double oldDist = sqrt(px * px + py * py + pz * pz);
-    const double k = (dist >= oldDist) ? s.sc->kout : s.sc->kin;
-
-    const double h = M.h_min;
-    const double coef = vdw_coef(h, Ra, Rb, twoRa, twoRb, fourRa, cR3a);
-    const double nx = rx / dist, ny = ry / dist, nz = rz / dist;  // normalized() == rVecab/dist
-    const double vdwx = coef * nx, vdwy = coef * ny, vdwz = coef * nz;
-    const double es = -k * overlap * .5;                          // :142
-    const double ex = es * nx, ey = es * ny, ez = es * nz;
-    const double gs = M.G * s.m[A] * s.m[B] / (dist * dist);      // :145
-    const double gx = gs * nx, gy = gs * ny, gz = gs * nz;
-
-    const double efm = sqrt(ex * ex + ey * ey + ez * ez);         // :154
-    const double rax = (rx * Ra) / sumRaRb, ray = (ry * Ra) / sumRaRb, raz = (rz * Ra) / sumRaRb;
-    const double rbx = (-rx * Rb) / sumRaRb, rby = (-ry * Rb) / sumRaRb, rbz = (-rz * Rb) / sumRaRb;
-    const double wax = s.w.c[0][A], way = s.w.c[1][A], waz = s.w.c[2][A];
-    const double wbx = s.w.c[0][B], wby = s.w.c[1][B], wbz = s.w.c[2][B];
-    const double wdx = wax - wbx, wdy = way - wby, wdz = waz - wbz;  // :157
-    const double dvx = s.vel.c[0][B] - s.vel.c[0][A];               // :160
-    const double dvy = s.vel.c[1][B] - s.vel.c[1][A];
-    const double dvz = s.vel.c[2][B] - s.vel.c[2][A];
-    // frame_A_vel_B, :161-162
-    const double dot = dvx * rx + dvy * ry + dvz * rz;
-    const double dd = dist * dist;
-    const double ux = rx / dd, uy = ry / dd, uz = rz / dd;
-    const double cax = way * raz - waz * ray, cay = waz * rax - wax * raz, caz = wax * ray - way * rax;
-    const double cbx = wby * raz - wbz * ray, cby = wbz * rax - wbx * raz, cbz = wbx * ray - wby * rax;
-    const double fvx = dvx - dot * ux - cax - cbx;
-    const double fvy = dvy - dot * uy - cay - cby;
-    const double fvz = dvz - dot * uz - caz - cbz;
-
-    double sx = 0, sy = 0, sz = 0;
-    const double rvm = sqrt(fvx * fvx + fvy * fvy + fvz * fvz);
-    if (rvm > 1e-13) {                                            // :166-170
-        const double ss = M.u_s * efm;
-        sx = ss * (fvx / rvm); sy = ss * (fvy / rvm); sz = ss * (fvz / rvm);
-    }
-    double qx = 0, qy = 0, qz = 0;
-    const double wdm = sqrt(wdx * wdx + wdy * wdy + wdz * wdz);
-    if (wdm > 1e-13) {                                            // :174-178
-        const double cx = wdy * raz - wdz * ray, cy = wdz * rax - wdx * raz, cz = wdx * ray - wdy * rax;
-        const double cn = sqrt(cx * cx + cy * cy + cz * cz);
-        const double rs = -M.u_r * efm;
-        qx = (rs * cx) / cn; qy = (rs * cy) / cn; qz = (rs * cz) / cn;
-    }
-    ContactOut o;
-    o.fx = gx + ex + sx + vdwx;                                   // :181
-    o.fy = gy + ey + sy + vdwy;
-    o.fz = gz + ez + sz + vdwz;
-    const double pax = sx + qx, pay = sy + qy, paz = sz + qz;     // :184
-    o.tax = ray * paz - raz * pay; o.tay = raz * pax - rax * paz; o.taz = rax * pay - ray * pax;
-    const double pbx = -sx + qx, pby = -sy + qy, pbz = -sz + qz;  // :185
-    o.tbx = rby * pbz - rbz * pby; o.tby = rbz * pbx - rbx * pbz; o.tbz = rbx * pby - rby * pbx;
-    o.pe = 0;
-    if (WRITE) o.pe = vdw_energy(M.Ha, h, Ra, Rb, twoRa) + 0.5 * k * overlap * overlap;  // :203
-    return o;
-}
-
 // One warp per lower-triangular 32x32 block tile (X, Y), X >= Y.  Lane b
 // owns sphere B = 32Y + b and walks the 32 spheres A = 32X + a of the A
-// block; on the diagonal only a > b is a pair.  Tiles are independent, so
-// the grid is a static stride over all tiles.
+// block; on the diagonal only a > b is a pair.  Tiles are independent; one
+// launch covers the tiles of block columns [c0, c1) with a static stride.
+// Tiles in column-major order: column Y holds tiles (Y..nb-1, Y); the first
+// tile of column c has index c*nb - c(c-1)/2.
+__device__ __forceinline__ long long col_offset(int nb, int c) { return (long long)c * nb - (long long)c * (c - 1) / 2; }
+
+__device__ __forceinline__ void col_tile_coords(int nb, long long u, int& X, int& Y)
+{
+    const double b = 2.0 * nb + 1.0;
+    int c = (int)((b - sqrt(b * b - 8.0 * (double)u)) * 0.5);
+    c = max(0, min(c, nb - 1));
+    while (c + 1 < nb && col_offset(nb, c + 1) <= u) ++c;
+    while (c > 0 && col_offset(nb, c) > u) --c;
+    Y = c;
+    X = c + (int)(u - col_offset(nb, c));
+}
+
 template <bool WRITE>
-__global__ void __launch_bounds__(128, 2) pair_tile_kernel(const __grid_constant__ System s)
+__global__ void __launch_bounds__(128, 3) pair_tile_kernel(const __grid_constant__ System s, int c0, int c1)
 {
     __shared__ ABlock sA[4];
     const int lane = threadIdx.x & 31;
@@ -169,9 +84,11 @@ __global__ void __launch_bounds__(128, 2) pair_tile_kernel(const __grid_constant
     const size_t plane = (size_t)s.npad * s.npad;
     const double Ha = s.mat.Ha, h_min = s.mat.h_min;
 
-    for (long long t = (long long)blockIdx.x * 4 + wib; t < s.ntiles; t += nwarps) {
+    const long long u1 = col_offset(s.nb, c1);
+    for (long long u = col_offset(s.nb, c0) + (long long)blockIdx.x * 4 + wib; u < u1; u += nwarps) {
         int X, Y;
-        tile_coords(t, X, Y);
+        col_tile_coords(s.nb, u, X, Y);
+        const long long t = (long long)X * (X + 1) / 2 + Y;  // this tile's PE slot
         {
             const int i = X * kBlock + lane;  // < npad always
             ab.x[lane] = s.pos.c[0][i]; ab.y[lane] = s.pos.c[1][i]; ab.z[lane] = s.pos.c[2][i];
@@ -197,13 +114,16 @@ __global__ void __launch_bounds__(128, 2) pair_tile_kernel(const __grid_constant
                 const double Ra = ab.R[a];
                 const double sumRaRb = Ra + Rb;                              // :104
                 const double rx = bx - ab.x[a], ry = by - ab.y[a], rz = bz - ab.z[a];  // :105
-                const double dist = sqrt(rx * rx + ry * ry + rz * rz);      // :107
+                const double d2 = rx * rx + ry * ry + rz * rz;
+                const double y = rsqrt_refined(d2);                           // ~1/dist
+                const double dist = sqrt_from_estimate(d2, d2 * y);           // :107, RN(sqrt)
                 const double overlap = sumRaRb - dist;                        // :110
                 double fx, fy, fz;
                 if (overlap > 0) {
                     contact = true;
-                    const ContactOut o = contact_pair<WRITE>(s, A, B, rx, ry, rz, dist, overlap, Ra, Rb,
-                                                             ab.twoR[a], twoRb, ab.fourR[a], ab.cR3[a]);
+                    const ContactIn in = gather_contact(s, A, B);
+                    const ContactOut o = contact_pair_exact<WRITE>(in, s.mat, rx, ry, rz, dist, overlap, Ra, Rb,
+                                                                   ab.twoR[a], twoRb, ab.fourR[a], ab.cR3[a]);
                     fx = o.fx; fy = o.fy; fz = o.fz;
                     const double im_a = s.inv_moi[A], mo_a = s.moi[A];
                     const double im_b = s.inv_moi[B], mo_b = s.moi[B];
@@ -220,19 +140,21 @@ __global__ void __launch_bounds__(128, 2) pair_tile_kernel(const __grid_constant
                     double h = fabs(overlap);                                  // :211-215
                     if (h < h_min) h = h_min;
                     const double coef = vdw_coef(h, Ra, Rb, ab.twoR[a], twoRb, ab.fourR[a], ab.cR3[a]);
-                    fx = coef * (rx / dist); fy = coef * (ry / dist); fz = coef * (rz / dist);  // :221-227
+                    fx = coef * div_from_estimate(rx, dist, rx * y);             // :221-227
+                    fy = coef * div_from_estimate(ry, dist, ry * y);
+                    fz = coef * div_from_estimate(rz, dist, rz * y);
                     if (WRITE) pe += vdw_energy(Ha, h, Ra, Rb, ab.twoR[a]);                    // :239
                 }
                 // :249-250 -- acc[A] += F/m[A]; acc[B] -= F/m[B] (stored negated)
                 const double ma = ab.m[a], ima = ab.inv_m[a];
                 double* pa = rowA + (size_t)a * s.npad;
-                __stcs(pa, div_by_recip(fx, ma, ima));
-                __stcs(pa + plane, div_by_recip(fy, ma, ima));
-                __stcs(pa + 2 * plane, div_by_recip(fz, ma, ima));
+                __stcs(pa, div_from_estimate(fx, ma, fx * ima));
+                __stcs(pa + plane, div_from_estimate(fy, ma, fy * ima));
+                __stcs(pa + 2 * plane, div_from_estimate(fz, ma, fz * ima));
                 double* pb = rowB + a;
-                __stcs(pb, -div_by_recip(fx, mb, inv_mb));
-                __stcs(pb + plane, -div_by_recip(fy, mb, inv_mb));
-                __stcs(pb + 2 * plane, -div_by_recip(fz, mb, inv_mb));
+                __stcs(pb, -div_from_estimate(fx, mb, fx * inv_mb));
+                __stcs(pb + plane, -div_from_estimate(fy, mb, fy * inv_mb));
+                __stcs(pb + 2 * plane, -div_from_estimate(fz, mb, fz * inv_mb));
             }
             const uint32_t bal = __ballot_sync(0xffffffffu, contact);
             if (lane == a) rowbits = bal;
@@ -255,15 +177,19 @@ __global__ void __launch_bounds__(128, 2) pair_tile_kernel(const __grid_constant
 }
 
 // ------------------------------------------------- row sums + pass 3 ------
-// Thread (c, i): acc_c[i] = sum over partners j ascending of pairbuf[c][i][j]
-// (j != i), aacc_c[i] likewise over the contact partners, then pass 3.
-// The sum is a dependent chain per (c, i), so the kernel is latency-bound:
-// each thread keeps kRowBatch 16-byte loads of its row in flight (register
-// double buffering) while it adds the previous batch.
+// Thread (c, i) continues acc_c[i] = sum over partners j ascending of
+// pairbuf[c][i][j] (j != i) over the partner blocks [b0, b1), and aacc_c[i]
+// likewise over the contact partners -- the order in which the reference
+// adds terms to acc[i] and aacc[i].  Between segments the running sums are
+// kept in acc/aacc (dead after the step's drift); the last segment does
+// pass 3.  The sum is a dependent chain per (c, i), so the kernel is
+// latency-bound: each thread keeps kRowBatch 16-byte loads in flight
+// (register double buffering) while it adds the previous batch.
 constexpr int kRowBatch = 16;
 constexpr int kRowThreads = 32;
 
-__global__ void __launch_bounds__(kRowThreads) rowsum_kernel(const __grid_constant__ System s)
+__global__ void __launch_bounds__(kRowThreads) rowsum_kernel(const __grid_constant__ System s, int b0, int b1,
+                                                             int first, int last)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 3 * s.n) return;
@@ -272,30 +198,31 @@ __global__ void __launch_bounds__(kRowThreads) rowsum_kernel(const __grid_consta
     const int n = s.n;
     const size_t plane = (size_t)s.npad * s.npad;
     const double2* row = reinterpret_cast<const double2*>(s.pairbuf + c * plane + (size_t)i * s.npad);
-    const int nv = (n + 1) / 2;  // double2 words covering columns [0, n)
+    const int j0 = b0 * kBlock, j1 = min(b1 * kBlock, n);
+    const int v0 = j0 / 2, v1 = (j1 + 1) / 2;  // double2 words covering columns [j0, j1)
     double2 cur[kRowBatch], nxt[kRowBatch];
 #pragma unroll
-    for (int k = 0; k < kRowBatch; ++k) cur[k] = k < nv ? __ldcs(row + k) : make_double2(0.0, 0.0);
-    double acc = 0.0;
-    for (int base = 0; base < nv; base += kRowBatch) {
+    for (int k = 0; k < kRowBatch; ++k) cur[k] = v0 + k < v1 ? __ldcs(row + v0 + k) : make_double2(0.0, 0.0);
+    double acc = first ? 0.0 : s.acc.c[c][i];
+    for (int base = v0; base < v1; base += kRowBatch) {
 #pragma unroll
         for (int k = 0; k < kRowBatch; ++k) {
             const int q = base + kRowBatch + k;
-            nxt[k] = q < nv ? __ldcs(row + q) : make_double2(0.0, 0.0);
+            nxt[k] = q < v1 ? __ldcs(row + q) : make_double2(0.0, 0.0);
         }
 #pragma unroll
         for (int k = 0; k < kRowBatch; ++k) {
             const int j = 2 * (base + k);
-            if (j < n && j != i) acc += cur[k].x;
-            if (j + 1 < n && j + 1 != i) acc += cur[k].y;
+            if (j < j1 && j != i) acc += cur[k].x;
+            if (j + 1 < j1 && j + 1 != i) acc += cur[k].y;
         }
 #pragma unroll
         for (int k = 0; k < kRowBatch; ++k) cur[k] = nxt[k];
     }
-    double aacc = 0.0;
+    double aacc = first ? 0.0 : s.aacc.c[c][i];
     const uint32_t* mrow = s.cmask + (size_t)i * s.nb;
     const double* trow = s.torqbuf + c * plane + (size_t)i * s.npad;
-    for (int Y = 0; Y < s.nb; ++Y) {
+    for (int Y = b0; Y < b1; ++Y) {
         uint32_t wd = mrow[Y];
         while (wd) {
             const int b = __ffs(wd) - 1;
@@ -303,11 +230,12 @@ __global__ void __launch_bounds__(kRowThreads) rowsum_kernel(const __grid_consta
             aacc += trow[Y * kBlock + b];
         }
     }
+    s.acc.c[c][i] = acc;
+    s.aacc.c[c][i] = aacc;
+    if (!last) return;
     const double dt = s.sc->dt;
     const double v = s.velh.c[c][i] + (.5 * acc) * dt;    // :265
     const double wv = s.wh.c[c][i] + (.5 * aacc) * dt;    // :266
-    s.acc.c[c][i] = acc;
-    s.aacc.c[c][i] = aacc;
     s.vel.c[c][i] = v;
     s.w.c[c][i] = wv;
     if (!isfinite(v) || !isfinite(wv) || !isfinite(s.pos.c[c][i])) atomicOr(s.status, 1u);
@@ -381,14 +309,34 @@ __global__ void derive_kernel(const __grid_constant__ System s)
     s.cR3[i] = s.mat.Ha / 6 * 64 * R * R * R;
     s.inv_m[i] = 1.0 / m;
     s.inv_moi[i] = 1.0 / moi;
+    if (s.f_R) {  // mixed-precision form: FP32 constants, lengths scaled by 2^-len_shift
+        s.f_R[i] = d2f_bits(R, s.len_shift);
+        s.f_inv_m[i] = d2f_bits(1.0 / m, 0);
+        s.f_inv_moi[i] = d2f_bits(1.0 / moi, 0);
+    }
 }
 
 // ------------------------------------------------------------ launchers --
-int pair_grid_blocks(const System& s, int num_sms)
+int pair_grid_blocks(long long tiles, int num_sms)
 {
-    long long want = (s.ntiles + 3) / 4;
-    long long cap = (long long)num_sms * 2;  // 2 CTAs (8 warps) per SM
+    long long want = (tiles + 3) / 4;
+    long long cap = (long long)num_sms * 3;  // 3 CTAs (12 warps) per SM
     return (int)(want < cap ? want : cap);
+}
+
+// Block-column boundaries of the pair phases: the row-sum segment over the
+// partner blocks of phase p runs on the side stream while phases p+1.. run;
+// phases shrink toward the end so that little of the last segment is exposed.
+int phase_bounds(int nb, int* cb)
+{
+    static const double frac[kPairPhases + 1] = {0.0, 1.0 / 3.0, 2.0 / 3.0, 0.85, 0.95, 1.0};
+    int np = 0;
+    cb[0] = 0;
+    for (int p = 1; p <= kPairPhases; ++p) {
+        const int c = p == kPairPhases ? nb : (int)(frac[p] * nb + 0.5);
+        if (c > cb[np]) cb[++np] = c;
+    }
+    return np;
 }
 
 void launch_derive(const System& s, cudaStream_t st)
@@ -396,24 +344,54 @@ void launch_derive(const System& s, cudaStream_t st)
     derive_kernel<<<(s.npad + 255) / 256, 256, 0, st>>>(s);
 }
 
-void launch_step(const System& s, bool write, int num_sms, cudaStream_t st, StepTimers* tm)
+void launch_drift(const System& s, cudaStream_t st)
 {
     drift_kernel<<<(s.n + 255) / 256, 256, 0, st>>>(s);
-    if (tm) cudaEventRecord(tm->ev[0], st);
-    const int pb = pair_grid_blocks(s, num_sms);
+}
+
+void launch_energy(const System& s, cudaStream_t st)
+{
+    const int nred = kRedBlocks;
+    const int chunk = (s.n + nred - 1) / nred;
+    energy_partial_kernel<<<nred, kRedThreads, 0, st>>>(s, chunk);
+    energy_final_kernel<<<1, kRedThreads, 0, st>>>(s, nred);
+}
+
+static void launch_pair_columns(const System& s, bool write, int num_sms, cudaStream_t st, int c0, int c1)
+{
+    const long long tiles = ((long long)c1 * s.nb - (long long)c1 * (c1 - 1) / 2) -
+                            ((long long)c0 * s.nb - (long long)c0 * (c0 - 1) / 2);
+    const int pb = pair_grid_blocks(tiles, num_sms);
     if (write)
-        pair_tile_kernel<true><<<pb, 128, 0, st>>>(s);
+        pair_tile_kernel<true><<<pb, 128, 0, st>>>(s, c0, c1);
     else
-        pair_tile_kernel<false><<<pb, 128, 0, st>>>(s);
-    if (tm) cudaEventRecord(tm->ev[1], st);
-    rowsum_kernel<<<(3 * s.n + kRowThreads - 1) / kRowThreads, kRowThreads, 0, st>>>(s);
-    if (tm) cudaEventRecord(tm->ev[2], st);
-    if (write) {
-        const int nred = kRedBlocks;
-        const int chunk = (s.n + nred - 1) / nred;
-        energy_partial_kernel<<<nred, kRedThreads, 0, st>>>(s, chunk);
-        energy_final_kernel<<<1, kRedThreads, 0, st>>>(s, nred);
+        pair_tile_kernel<false><<<pb, 128, 0, st>>>(s, c0, c1);
+}
+
+void launch_step(const System& s, bool write, int num_sms, cudaStream_t st, StepTimers* tm, const StepOverlap* ov)
+{
+    launch_drift(s, st);
+    if (tm) cudaEventRecord(tm->ev[0], st);
+    const int rb = (3 * s.n + kRowThreads - 1) / kRowThreads;
+    int cb[kPairPhases + 1];
+    const int np = ov ? phase_bounds(s.nb, cb) : 1;
+    if (np <= 1) {
+        launch_pair_columns(s, write, num_sms, st, 0, s.nb);
+        if (tm) cudaEventRecord(tm->ev[1], st);
+        rowsum_kernel<<<rb, kRowThreads, 0, st>>>(s, 0, s.nb, 1, 1);
+    } else {
+        for (int p = 0; p < np; ++p) {
+            launch_pair_columns(s, write, num_sms, st, cb[p], cb[p + 1]);
+            cudaEventRecord(ov->phase[p], st);
+            cudaStreamWaitEvent(ov->side, ov->phase[p], 0);
+            rowsum_kernel<<<rb, kRowThreads, 0, ov->side>>>(s, cb[p], cb[p + 1], p == 0, p == np - 1);
+        }
+        if (tm) cudaEventRecord(tm->ev[1], st);
+        cudaEventRecord(ov->join, ov->side);
+        cudaStreamWaitEvent(st, ov->join, 0);
     }
+    if (tm) cudaEventRecord(tm->ev[2], st);
+    if (write) launch_energy(s, st);
 }
 
 }  // namespace sl

@@ -1,0 +1,209 @@
+// sl_step_mixed.cu -- the mixed-precision form of the step (SL_MODE_MIXED).
+//
+// FP64 is kept where precision is set:
+//   * positions and the whole integration (drift_kernel, shared with the
+//     exact form; pass 3 in mixed_rowsum_kernel);
+//   * the pair subtraction r = pos[B] - pos[A], |r|^2 and the squared gap
+//     g = (R_A + R_B)^2 - |r|^2, from which the overlap is taken as
+//     g / (R_A + R_B + |r|) -- no cancellation in R_A + R_B - |r|;
+//   * the previous-step distance test that chooses kin or kout;
+//   * per-sphere force and torque accumulation: each sphere's FP32 pair
+//     terms are added into an FP64 sum in ascending partner order;
+//   * the write-step potential energy per pair and the energy totals.
+// Everything else -- distances, the vdW coefficient, elastic, gravity,
+// sliding and rolling friction, torques -- is FP32 on lengths scaled by
+// 2^-len_shift (about one radius), which keeps R^6 / (S^2 T^2) far from
+// FP32's range limits.  Float <-> double conversions are bit manipulation
+// on the integer pipe (f2d_bits / d2f_bits), so the FP64 pipe carries only
+// 8 operations per pair in the pair pass and 6 in the sums.
+// The physics follows ColliderSingleCore.cpp:104-253 term by term; only the
+// arithmetic and the evaluation order differ.
+#include "sl_device.cuh"
+#include "sl_kernels.h"
+#include "sl_pair_mixed.cuh"
+
+namespace sl {
+
+namespace {
+
+struct ABlockMixed {
+    double x[kBlock], y[kBlock], z[kBlock], R[kBlock];
+    float Rs[kBlock], inv_m[kBlock];
+};
+
+// Same tiling as pair_tile_kernel: one warp per lower-triangular 32x32 block
+// tile, lane b = sphere 32Y+b, loop over the A block; terms stored as FP32
+// in the [3][npad][npad] float view of pairbuf/torqbuf.
+template <bool WRITE>
+__global__ void __launch_bounds__(128, 3) mixed_pair_kernel(const __grid_constant__ System s)
+{
+    __shared__ ABlockMixed sA[4];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    ABlockMixed& ab = sA[wib];
+    const long long nwarps = (long long)gridDim.x * 4;
+    const size_t plane = (size_t)s.npad * s.npad;
+    float* pbuf = reinterpret_cast<float*>(s.pairbuf);
+    float* tbuf = reinterpret_cast<float*>(s.torqbuf);
+    const int sh = s.len_shift;
+    const float L = ldexpf(1.0f, sh);
+    const float hmin_s = (float)s.mat.h_min / L;
+    const float c_vdw = (float)(s.mat.Ha / 6 * 64) / L;   // dyn per unit vdw_shape
+
+    for (long long t = (long long)blockIdx.x * 4 + wib; t < s.ntiles; t += nwarps) {
+        int X, Y;
+        tile_coords(t, X, Y);
+        {
+            const int i = X * kBlock + lane;
+            ab.x[lane] = s.pos.c[0][i]; ab.y[lane] = s.pos.c[1][i]; ab.z[lane] = s.pos.c[2][i];
+            ab.R[lane] = s.R[i]; ab.Rs[lane] = s.f_R[i]; ab.inv_m[lane] = s.f_inv_m[i];
+        }
+        __syncwarp();
+        const int B = Y * kBlock + lane;
+        const bool bvalid = B < s.n;
+        const double bx = s.pos.c[0][B], by = s.pos.c[1][B], bz = s.pos.c[2][B], Rb = s.R[B];
+        const float Rbs = s.f_R[B], inv_mb = s.f_inv_m[B];
+        const int a_end = min(kBlock, s.n - X * kBlock);
+        double pe = 0;
+        uint32_t rowbits = 0, colbits = 0;
+        float* rowA = pbuf + (size_t)(X * kBlock) * s.npad + B;
+        float* rowB = pbuf + (size_t)B * s.npad + X * kBlock;
+        for (int a = 0; a < a_end; ++a) {
+            const bool valid = bvalid && (X != Y || lane < a);
+            bool contact = false;
+            if (valid) {
+                const int A = X * kBlock + a;
+                // FP64: subtraction, |r|^2, squared gap
+                const double rx = bx - ab.x[a], ry = by - ab.y[a], rz = bz - ab.z[a];
+                const double d2 = fma(rx, rx, fma(ry, ry, rz * rz));
+                const double sum = ab.R[a] + Rb;
+                const double gap2 = fma(sum, sum, -d2);
+                // FP32 (scaled lengths)
+                const float rxs = d2f_bits(rx, sh), rys = d2f_bits(ry, sh), rzs = d2f_bits(rz, sh);
+                const float d2s = d2f_bits(d2, 2 * sh);
+                const float inv_d = rsqrtf(d2s);
+                const float dist_s = d2s * inv_d;
+                const float Ras = ab.Rs[a];
+                const float ovl_s = d2f_bits(gap2, 2 * sh) / (Ras + Rbs + dist_s);
+                const float nx = rxs * inv_d, ny = rys * inv_d, nz = rzs * inv_d;
+                float fx, fy, fz;
+                if (gap2 > 0.0) {
+                    contact = true;
+                    const ContactIn in = gather_contact(s, A, B);
+                    const ContactF o = contact_mixed(in, s.mat, sh, d2, nx, ny, nz, dist_s * L, ovl_s * L, Ras, Rbs);
+                    fx = o.fx; fy = o.fy; fz = o.fz;
+                    const float ima = s.f_inv_moi[A], imb = s.f_inv_moi[B];
+                    float* ta = tbuf + (size_t)A * s.npad + B;
+                    float* tb = tbuf + (size_t)B * s.npad + A;
+                    ta[0] = o.tax * ima; ta[plane] = o.tay * ima; ta[2 * plane] = o.taz * ima;
+                    tb[0] = o.tbx * imb; tb[plane] = o.tby * imb; tb[2 * plane] = o.tbz * imb;
+                    if (WRITE) pe += pair_pe_fp64(s.mat, ab.R[a], Rb, gap2, d2, true, o.k);
+                } else {
+                    const float h = fmaxf(-ovl_s, hmin_s);                  // :211-215
+                    const float f = c_vdw * vdw_shape(h, Ras, Rbs);
+                    fx = f * nx; fy = f * ny; fz = f * nz;
+                    if (WRITE) pe += pair_pe_fp64(s.mat, ab.R[a], Rb, gap2, d2, false, 0.0);
+                }
+                const float ima = ab.inv_m[a];
+                float* pa = rowA + (size_t)a * s.npad;
+                __stcs(pa, fx * ima); __stcs(pa + plane, fy * ima); __stcs(pa + 2 * plane, fz * ima);
+                float* pb = rowB + a;
+                __stcs(pb, -fx * inv_mb); __stcs(pb + plane, -fy * inv_mb); __stcs(pb + 2 * plane, -fz * inv_mb);
+            }
+            const uint32_t bal = __ballot_sync(0xffffffffu, contact);
+            if (lane == a) rowbits = bal;
+            if (contact) colbits |= 1u << a;
+        }
+        if (X == Y) {
+            s.cmask[(size_t)(X * kBlock + lane) * s.nb + X] = rowbits | colbits;
+        } else {
+            s.cmask[(size_t)(X * kBlock + lane) * s.nb + Y] = rowbits;
+            s.cmask[(size_t)(Y * kBlock + lane) * s.nb + X] = colbits;
+        }
+        if (WRITE) {
+            for (int off = 16; off > 0; off >>= 1) pe += __shfl_xor_sync(0xffffffffu, pe, off);
+            if (lane == 0) s.pe_tile[t] = pe;
+        }
+        __syncwarp();
+    }
+}
+
+constexpr int kMixBatch = 8;  // float4 loads in flight per thread
+constexpr int kMixThreads = 32;
+
+// Thread (c, i): FP64 sum of the FP32 terms of row i in ascending partner
+// order, torque terms of contact partners likewise, then pass 3 in FP64.
+__global__ void __launch_bounds__(kMixThreads) mixed_rowsum_kernel(const __grid_constant__ System s)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 3 * s.n) return;
+    const int c = t / s.n;
+    const int i = t - c * s.n;
+    const int n = s.n;
+    const size_t plane = (size_t)s.npad * s.npad;
+    const float* rowf = reinterpret_cast<const float*>(s.pairbuf) + c * plane + (size_t)i * s.npad;
+    const float4* row = reinterpret_cast<const float4*>(rowf);
+    const int nv = (n + 3) / 4;
+    float4 cur[kMixBatch], nxt[kMixBatch];
+    const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < kMixBatch; ++k) cur[k] = k < nv ? __ldcs(row + k) : zero4;
+    double acc = 0.0;
+    for (int base = 0; base < nv; base += kMixBatch) {
+#pragma unroll
+        for (int k = 0; k < kMixBatch; ++k) {
+            const int q = base + kMixBatch + k;
+            nxt[k] = q < nv ? __ldcs(row + q) : zero4;
+        }
+#pragma unroll
+        for (int k = 0; k < kMixBatch; ++k) {
+            const int j = 4 * (base + k);
+            const float v[4] = {cur[k].x, cur[k].y, cur[k].z, cur[k].w};
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (j + u < n && j + u != i) acc += f2d_bits(v[u]);
+        }
+#pragma unroll
+        for (int k = 0; k < kMixBatch; ++k) cur[k] = nxt[k];
+    }
+    double aacc = 0.0;
+    const uint32_t* mrow = s.cmask + (size_t)i * s.nb;
+    const float* trow = reinterpret_cast<const float*>(s.torqbuf) + c * plane + (size_t)i * s.npad;
+    for (int Y = 0; Y < s.nb; ++Y) {
+        uint32_t wd = mrow[Y];
+        while (wd) {
+            const int b = __ffs(wd) - 1;
+            wd &= wd - 1;
+            aacc += f2d_bits(trow[Y * kBlock + b]);
+        }
+    }
+    const double dt = s.sc->dt;
+    const double v = s.velh.c[c][i] + (.5 * acc) * dt;
+    const double wv = s.wh.c[c][i] + (.5 * aacc) * dt;
+    s.acc.c[c][i] = acc;
+    s.aacc.c[c][i] = aacc;
+    s.vel.c[c][i] = v;
+    s.w.c[c][i] = wv;
+    if (!isfinite(v) || !isfinite(wv) || !isfinite(s.pos.c[c][i])) atomicOr(s.status, 1u);
+}
+
+}  // namespace
+
+void launch_step_mixed(const System& s, bool write, int num_sms, cudaStream_t st, StepTimers* tm)
+{
+    launch_drift(s, st);
+    if (tm) cudaEventRecord(tm->ev[0], st);
+    long long want = (s.ntiles + 3) / 4;
+    long long cap = (long long)num_sms * 3;
+    const int pb = (int)(want < cap ? want : cap);
+    if (write)
+        mixed_pair_kernel<true><<<pb, 128, 0, st>>>(s);
+    else
+        mixed_pair_kernel<false><<<pb, 128, 0, st>>>(s);
+    if (tm) cudaEventRecord(tm->ev[1], st);
+    mixed_rowsum_kernel<<<(3 * s.n + kMixThreads - 1) / kMixThreads, kMixThreads, 0, st>>>(s);
+    if (tm) cudaEventRecord(tm->ev[2], st);
+    if (write) launch_energy(s, st);
+}
+
+}  // namespace sl

@@ -189,6 +189,43 @@ def test_looper_graph_matches_single_steps():
         assert np.array_equal(sa[key], sb[key])
 
 
+@pytest.mark.parametrize("n", [20, 40, 300, 1000])
+def test_pipelined_step_matches_sequential(n):
+    """Row sums run per block-column phase beside the later pair phases
+    (1 phase at n=20, 2 at n=40, 5 at n>=300); the sums keep their order, so
+    single steps and the graph-captured looper equal the one-launch step
+    bit for bit and the oracle stays bit-identical."""
+    c = contact_case(n, 300 + n)
+    a, b = _gpu(c), _gpu(c)
+    b.set_overlap(False)
+    o = _oracle(c)
+    a.init_conditions(); b.init_conditions(); o.init()
+    for step in range(1, 21):
+        ea = a.sim_one_step(step % 5 == 0)
+        eb = b.sim_one_step(step % 5 == 0)
+        o.step(step % 5 == 0)
+        if ea is not None:
+            assert ea.as_array().tolist() == eb.as_array().tolist()
+    sa, sb, so = _state(a), _state(b), o.state()
+    for key in STATE_KEYS:
+        assert np.array_equal(sa[key], sb[key]), key
+        assert np.array_equal(sa[key], so[key]), key
+    ra = a.sim_looper(steps=41, skip=10, first_step=21)
+    rb = b.sim_looper(steps=41, skip=10, first_step=21)
+    assert [r.PE for r in ra] == [r.PE for r in rb] and [r.KE for r in ra] == [r.KE for r in rb]
+    sa, sb = _state(a), _state(b)
+    for key in STATE_KEYS:
+        assert np.array_equal(sa[key], sb[key]), key
+
+
+def test_mixed_mode_has_no_pipelined_step():
+    c = contact_case(64, 5)
+    s = _gpu(c, "mixed")
+    s.set_overlap(False)
+    with pytest.raises(SpaceLabError):
+        s.set_overlap(True)
+
+
 def test_resume_matches_continuous_run():
     c = contact_case(128, 31)
     a = _gpu(c)
@@ -250,3 +287,31 @@ def test_bad_inputs_rejected():
     c["pos"][2, 1] = np.nan
     with pytest.raises(SpaceLabError):
         _gpu(c)
+
+
+def test_integer_rounded_quotient_and_sqrt_are_ieee_exact():
+    """The step kernels' quotients and square roots (FP64 estimate + exact
+    integer rounding, with hardware fallback) equal the IEEE results bit for
+    bit: random operands over wide exponent ranges, quotients next to
+    midpoints and binade edges, signed zeros and the physics' own ranges."""
+    lib = _lib.lib()
+    rng = np.random.default_rng(7)
+    n = 1 << 21
+    a = rng.normal(0, 1, n) * 10.0 ** rng.uniform(-30, 30, n)
+    b = rng.normal(0, 1, n) * 10.0 ** rng.uniform(-18, 18, n)
+    k = n // 8
+    b[:k] = np.nextafter(2.0 ** rng.integers(-60, 60, k), 0)               # all-ones significands
+    b[k:2 * k] = 2.0 ** rng.integers(-60, 60, k) * (1 + 2.0 ** -52)        # 1 + ulp
+    a[2 * k:3 * k] = b[2 * k:3 * k] * (1 + rng.integers(1, 1 << 20, k) * 2.0 ** -53)  # near midpoints
+    a[3 * k:4 * k] = rng.uniform(1e-6, 3e-3, k)                              # displacements (cm)
+    b[3 * k:4 * k] = rng.uniform(1e-4, 3e-3, k)                              # distances
+    a[4 * k:5 * k] = rng.normal(0, 1e-8, k)                                  # forces (dyn)
+    b[4 * k:5 * k] = rng.uniform(1e-12, 6e-11, k)                            # masses (g)
+    a[5 * k:5 * k + 8] = [0.0, -0.0, 1.0, -1.0, 2.0 ** -1022, 1e308, 4.0, 9.0]
+    out = np.zeros(4 * n)
+    assert lib.sl_diag_exact_ops(n, _lib.dptr(a), _lib.dptr(b), _lib.dptr(out)) == 0
+    fast_q, hw_q, fast_s, hw_s = out.reshape(4, n)
+    assert np.array_equal(hw_q, a / b, equal_nan=True)
+    assert np.array_equal(fast_q.view(np.int64), hw_q.view(np.int64))
+    assert np.array_equal(hw_s, np.sqrt(np.abs(a)))
+    assert np.array_equal(fast_s.view(np.int64), hw_s.view(np.int64))
