@@ -188,6 +188,8 @@ def run_ours(args, rank, world, local_rank) -> dict | None:
     w = _workload(args.workload)
     g = w.group
     sim = GpuStep(g.copy(), w.material, args.mode)
+    if args.overlap:
+        sim.set_overlap(True)
     sim.set_scalars(w.dt, w.kin, w.kout)
     sim.init_conditions()
     stream = torch.cuda.ExternalStream(sim.stream_ptr())
@@ -249,7 +251,8 @@ def run_ours(args, rank, world, local_rank) -> dict | None:
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64" if args.mode == "exact" else "f32+f64",
         "data": "synthetic (seeded clusters; no dataset)",
-        "config": _config(w, {"parallelism": "replicas" if world > 1 else "single GPU", "mode": args.mode}),
+        "config": _config(w, {"parallelism": "replicas" if world > 1 else "single GPU", "mode": args.mode,
+                               "overlap": bool(args.overlap)}),
         "impl": "ours",
         "e2e": e2e,
         "gpu_launches": gpu_launches,
@@ -456,6 +459,8 @@ def main(argv=None) -> int:
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU oracle timing (rank 0)")
     ap.add_argument("--mode", choices=["exact", "mixed"], default="exact")
+    ap.add_argument("--overlap", action="store_true",
+                    help="exact mode: run the row sums beside the pair phases (sl_set_overlap)")
     ap.add_argument("--workload", choices=WORKLOADS, default="aggregate_collision_n5000")
     ap.add_argument("--drift-steps", type=int, default=0,
                     help="instead of the benchmark: run the mixed and the FP64 form side by side for this many "

@@ -21,6 +21,13 @@ int sl_diag_division(int n, const double* a, const double* b, double* q_recip, d
  * IEEE results.  Host arrays; out has 4n entries. */
 int sl_diag_exact_ops(int n, const double* a, const double* b, double* out);
 
+/* The integer-pipe estimates of the exact step, rounded exactly: out[4n]
+ * = a/b with a fixed-point reciprocal of b made at set-up, a/b with a
+ * Newton fixed-point reciprocal, sqrt(|a|) from a fixed-point 1/sqrt, and
+ * a / RN(sqrt(|b|)) from the fixed-point 1/sqrt of |b|.  Each must equal
+ * the IEEE result bit for bit.  No reference counterpart (a self-test). */
+int sl_diag_int_ops(int n, const double* a, const double* b, double* out);
+
 /* Measured FP64 fused-multiply-add throughput of the current GPU in
  * GFLOP/s (2 flops per FMA), from a kernel of independent FMA chains timed
  * with CUDA events. */

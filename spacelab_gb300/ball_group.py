@@ -219,7 +219,7 @@ class GpuStep:
         return int(self._lib.sl_stream(self._h) or 0)
 
     def set_overlap(self, enable: bool) -> None:
-        """Exact mode: pipeline the row sums with the pair phases (default on)."""
+        """Exact mode: pipeline the row sums with the pair phases (default off)."""
         check(self._lib.sl_set_overlap(self._h, int(enable)), "sl_set_overlap")
 
     def step_launches(self, write: bool) -> int:

@@ -48,7 +48,8 @@ __device__ double pair_pass(const Batch& b, int off, int n, const Material& M, d
         const int gi = off + (active ? i : 0);
         const double xi = b.pos.c[0][gi], yi = b.pos.c[1][gi], zi = b.pos.c[2][gi];
         const double Ri = b.R[gi], twoRi = b.twoR[gi], fourRi = b.fourR[gi], cR3i = b.cR3[gi];
-        const double mi = b.m[gi], imi = b.inv_m[gi], moii = b.moi[gi], imoii = b.inv_moi[gi];
+        const double mi = b.m[gi], moii = b.moi[gi], imoii = b.inv_moi[gi];
+        const unsigned long long rmi = b.rm[gi];
         double ax = 0, ay = 0, az = 0, tx = 0, ty = 0, tz = 0;
         for (int jbase = 0; jbase < n; jbase += TILE) {
             for (int t = threadIdx.x; t < TILE; t += blockDim.x) {
@@ -74,8 +75,10 @@ __device__ double pair_pass(const Batch& b, int off, int n, const Material& M, d
                     const double sumRaRb = RA + RB;                                  // :104
                     const double rx = Bx - Ax, ry = By - Ay, rz = Bz - Az;           // :105
                     const double d2 = rx * rx + ry * ry + rz * rz;
-                    const double y = rsqrt_refined(d2);
-                    const double dist = sqrt_from_estimate(d2, d2 * y);              // :107
+                    int p;
+                    unsigned long long F;
+                    const unsigned long long Y = rsqrt_fix(d2, p, F);
+                    const double dist = sqrt_fix(d2, F, Y, p);                       // :107
                     const double overlap = sumRaRb - dist;                           // :110
                     double fx, fy, fz;
                     if (overlap > 0) {
@@ -98,15 +101,15 @@ __device__ double pair_pass(const Batch& b, int off, int n, const Material& M, d
                     } else {
                         double h = fabs(overlap);                                    // :211-215
                         if (h < M.h_min) h = M.h_min;
-                        const double coef = vdw_coef(h, RA, RB, twoRA, twoRB, fourRA, cR3A);
-                        fx = coef * div_from_estimate(rx, dist, rx * y);
-                        fy = coef * div_from_estimate(ry, dist, ry * y);
-                        fz = coef * div_from_estimate(rz, dist, rz * y);
+                        const double coef = vdw_coef_fix(h, RA, RB, twoRA, twoRB, fourRA, cR3A);
+                        fx = coef * div_by_rsqrt(rx, dist, Y, p);
+                        fy = coef * div_by_rsqrt(ry, dist, Y, p);
+                        fz = coef * div_by_rsqrt(rz, dist, Y, p);
                         if (WRITE && iA) pe += vdw_energy(M.Ha, h, RA, RB, twoRA);
                     }
-                    const double qx = div_from_estimate(fx, mi, fx * imi);           // :249-250
-                    const double qy = div_from_estimate(fy, mi, fy * imi);
-                    const double qz = div_from_estimate(fz, mi, fz * imi);
+                    const double qx = div_by_fixed<false>(fx, mi, rmi);              // :249-250
+                    const double qy = div_by_fixed<false>(fy, mi, rmi);
+                    const double qz = div_by_fixed<false>(fz, mi, rmi);
                     if (iA) { ax += qx; ay += qy; az += qz; }
                     else { ax -= qx; ay -= qy; az -= qz; }
                 }
@@ -174,7 +177,7 @@ __global__ void batch_derive_kernel(const __grid_constant__ Batch b)
     b.twoR[i] = 2 * R;
     b.fourR[i] = 4 * R;
     b.cR3[i] = b.mat.Ha / 6 * 64 * R * R * R;
-    b.inv_m[i] = 1.0 / m;
+    b.rm[i] = recip_of(m);
     b.inv_moi[i] = 1.0 / moi;
     if (b.f_R) {
         b.f_R[i] = d2f_bits(R, b.len_shift);

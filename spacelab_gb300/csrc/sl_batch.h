@@ -21,7 +21,9 @@ struct Batch {
     const double* kout;
     const double* u_s;    // per-instance sliding friction
     Vec3Soa pos, prev, vel, velh, w, wh, acc, aacc;
-    double *R, *m, *moi, *twoR, *fourR, *cR3, *inv_m, *inv_moi;
+    double *R, *m, *moi, *twoR, *fourR, *cR3;
+    unsigned long long* rm;  // 64-bit fixed-point reciprocal significand of m (recip_sig)
+    double* inv_moi;
     float *f_R, *f_inv_m, *f_inv_moi;  // mixed form (lengths scaled by 2^-len_shift)
     int len_shift;
     Material mat;         // G, Ha, u_r, h_min shared; u_s per instance

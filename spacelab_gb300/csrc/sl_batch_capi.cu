@@ -161,8 +161,10 @@ int sl_batch_create(int ninst, const int* counts, const sl_material* mat, int mo
     sl::Vec3Soa* vecs[8] = {&b.pos, &b.prev, &b.vel, &b.velh, &b.w, &b.wh, &b.acc, &b.aacc};
     for (int v = 0; v < 8; ++v)
         for (int c = 0; c < 3; ++c) vecs[v]->c[c] = reinterpret_cast<double*>(base + o_vec[v][c]);
-    double** scal[8] = {&b.R, &b.m, &b.moi, &b.twoR, &b.fourR, &b.cR3, &b.inv_m, &b.inv_moi};
+    double* inv_m_slot = nullptr;  // 8 bytes per sphere, holds the mass reciprocals rm
+    double** scal[8] = {&b.R, &b.m, &b.moi, &b.twoR, &b.fourR, &b.cR3, &inv_m_slot, &b.inv_moi};
     for (int k = 0; k < 8; ++k) *scal[k] = reinterpret_cast<double*>(base + o_sc[k]);
+    b.rm = reinterpret_cast<unsigned long long*>(inv_m_slot);
     if (mode == SL_MODE_MIXED) {
         b.f_R = reinterpret_cast<float*>(base + o_f[0]);
         b.f_inv_m = reinterpret_cast<float*>(base + o_f[1]);

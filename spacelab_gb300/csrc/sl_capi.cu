@@ -61,6 +61,8 @@ struct sl_handle {
     cudaStream_t stream = nullptr;
     // exact mode: side stream + events overlapping row sums with pair phases
     sl::StepOverlap ov{};
+    CUtensorMap pair_map{};  // exact mode: the pair-term buffer for the TMA row sums
+    bool has_map = false;
     bool has_ov = false;   // ov's stream and events exist
     bool overlap = false;  // steps use them
     void* arena = nullptr;
@@ -94,7 +96,8 @@ void launch_mode_step(sl_handle* h, bool write, sl::StepTimers* tm)
     if (h->mode == SL_MODE_MIXED)
         sl::launch_step_mixed(h->sys, write, h->num_sms, h->stream, tm);
     else
-        sl::launch_step(h->sys, write, h->num_sms, h->stream, tm, h->overlap ? &h->ov : nullptr);
+        sl::launch_step(h->sys, write, h->num_sms, h->stream, tm, h->overlap ? &h->ov : nullptr,
+                        h->has_map ? &h->pair_map : nullptr);
 }
 
 // One step on the handle's stream, with optional timing events.
@@ -129,6 +132,8 @@ int fetch_energy_and_status(sl_handle* h, sl_energy* out, bool want_energy)
             out->ang_mom[k] = h->h_energy[5 + k];
         }
     }
+    if (*h->h_status & sl::kStatusWaitTimeoutBit)
+        return fail(SL_ERR_CUDA, "a row-sum kernel's bounded wait for its TMA copies ran out");
     if (*h->h_status) return fail(SL_ERR_NONFINITE, "state became non-finite (NaN/Inf position, velocity or spin)");
     return SL_OK;
 }
@@ -203,7 +208,6 @@ int sl_create(int n, const sl_material* mat, int mode, sl_handle** out)
             e = cudaEventCreateWithFlags(&h->ov.phase[p], cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ov.join, cudaEventDisableTiming);
         if (e != cudaSuccess) { sl_destroy(h); return cuda_fail(e, "side stream / event creation"); }
-        h->overlap = true;
     }
 
     sl::System& s = h->sys;
@@ -239,8 +243,10 @@ int sl_create(int n, const sl_material* mat, int mode, sl_handle** out)
     sl::Vec3Soa* vecs[8] = {&s.pos, &s.prev, &s.vel, &s.velh, &s.w, &s.wh, &s.acc, &s.aacc};
     for (int v = 0; v < 8; ++v)
         for (int c = 0; c < 3; ++c) vecs[v]->c[c] = reinterpret_cast<double*>(base + o_vec[v][c]);
-    double** scal[8] = {&s.R, &s.m, &s.moi, &s.twoR, &s.fourR, &s.cR3, &s.inv_m, &s.inv_moi};
+    double* inv_m_slot = nullptr;  // 8 bytes per sphere, holds the mass reciprocals rm
+    double** scal[8] = {&s.R, &s.m, &s.moi, &s.twoR, &s.fourR, &s.cR3, &inv_m_slot, &s.inv_moi};
     for (int k = 0; k < 8; ++k) *scal[k] = reinterpret_cast<double*>(base + o_sc[k]);
+    s.rm = reinterpret_cast<unsigned long long*>(inv_m_slot);
     if (mode == SL_MODE_MIXED) {
         s.f_R = reinterpret_cast<float*>(base + o_f[0]);
         s.f_inv_m = reinterpret_cast<float*>(base + o_f[1]);
@@ -255,6 +261,7 @@ int sl_create(int n, const sl_material* mat, int mode, sl_handle** out)
     s.status = reinterpret_cast<unsigned int*>(base + o_st);
     h->d_sc = reinterpret_cast<sl::Scalars*>(base + o_scl);
     s.sc = h->d_sc;
+    if (mode == SL_MODE_EXACT) h->has_map = sl::make_pair_map(s, &h->pair_map);
     e = cudaMemsetAsync(h->arena, 0, h->arena_bytes, h->stream);
     if (e != cudaSuccess) { sl_destroy(h); return cuda_fail(e, "cudaMemset"); }
     e = cudaMallocHost(&h->staging, 18 * np * sizeof(double));

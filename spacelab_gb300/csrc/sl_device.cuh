@@ -41,7 +41,9 @@ struct System {
     int n, npad, nb;
     long long ntiles;  // nb * (nb + 1) / 2 lower-triangular block tiles
     Vec3Soa pos, prev, vel, velh, w, wh, acc, aacc;
-    double *R, *m, *moi, *twoR, *fourR, *cR3, *inv_m, *inv_moi;
+    double *R, *m, *moi, *twoR, *fourR, *cR3;
+    unsigned long long* rm;  // 64-bit fixed-point reciprocal significand of m (recip_sig)
+    double* inv_moi;
     double* pairbuf;      // [3][npad][npad]
     double* torqbuf;      // [3][npad][npad]
     uint32_t* cmask;      // [npad][nb]

@@ -33,6 +33,36 @@ __global__ void exact_ops_kernel(int n, const double* a, const double* b, double
     out[3 * (size_t)n + i] = sqrt(ax);
 }
 
+// out[0..n): a / b with the fixed-point reciprocal made at set-up
+// (recip_sig), [n..2n): a / b with the Newton reciprocal, [2n..3n):
+// sqrt(|a|) from the fixed-point 1/sqrt, [3n..4n): a / RN(sqrt(|b|)) from
+// the same 1/sqrt of |b|.
+__global__ void int_ops_kernel(int n, const double* a, const double* b, const unsigned long long* rb, double* out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double x = a[i], y = b[i];
+    out[i] = sl::div_by_fixed<false>(x, y, rb[i]);
+    out[n + i] = sl::div_by_fixed<true>(x, y, sl::recip_newton(y));
+    int p;
+    unsigned long long F;
+    const double ax = fabs(x);
+    const unsigned long long Y = sl::rsqrt_fix(ax, p, F);
+    out[2 * (size_t)n + i] = sl::sqrt_fix(ax, F, Y, p);
+    const double ay = fabs(y);
+    int q;
+    unsigned long long G;
+    const unsigned long long Z = sl::rsqrt_fix(ay, q, G);
+    const double d = sl::sqrt_fix(ay, G, Z, q);
+    out[3 * (size_t)n + i] = sl::div_by_rsqrt(x, d, Z, q);
+}
+
+__global__ void recip_kernel(int n, const double* b, unsigned long long* rb)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) rb[i] = sl::recip_of(b[i]);
+}
+
 constexpr int kChains = 8;
 constexpr int kIters = 4096;
 
@@ -88,6 +118,28 @@ extern "C" int sl_diag_exact_ops(int n, const double* a, const double* b, double
         rc = SL_ERR_CUDA;
     if (rc == SL_OK) {
         exact_ops_kernel<<<(n + 255) / 256, 256>>>(n, d, d + n, d + 2 * (size_t)n);
+        if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) rc = SL_ERR_CUDA;
+    }
+    if (rc == SL_OK && cudaMemcpy(out, d + 2 * (size_t)n, 4 * bytes, cudaMemcpyDeviceToHost) != cudaSuccess)
+        rc = SL_ERR_CUDA;
+    cudaFree(d);
+    return rc;
+}
+
+extern "C" int sl_diag_int_ops(int n, const double* a, const double* b, double* out)
+{
+    if (n < 1 || !a || !b || !out) return SL_ERR_ARG;
+    double* d = nullptr;
+    const size_t bytes = (size_t)n * sizeof(double);
+    if (cudaMalloc(&d, 7 * bytes) != cudaSuccess) return SL_ERR_ALLOC;
+    unsigned long long* rb = reinterpret_cast<unsigned long long*>(d + 6 * (size_t)n);
+    int rc = SL_OK;
+    if (cudaMemcpy(d, a, bytes, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(d + n, b, bytes, cudaMemcpyHostToDevice) != cudaSuccess)
+        rc = SL_ERR_CUDA;
+    if (rc == SL_OK) {
+        recip_kernel<<<(n + 255) / 256, 256>>>(n, d + n, rb);
+        int_ops_kernel<<<(n + 255) / 256, 256>>>(n, d, d + n, rb, d + 2 * (size_t)n);
         if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) rc = SL_ERR_CUDA;
     }
     if (rc == SL_OK && cudaMemcpy(out, d + 2 * (size_t)n, 4 * bytes, cudaMemcpyDeviceToHost) != cudaSuccess)

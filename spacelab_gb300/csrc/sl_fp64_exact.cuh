@@ -21,6 +21,7 @@
 // against the hardware operations in tests/test_gpu_parity.py.
 #pragma once
 #include <cstdint>
+#include <cstring>
 #include <cuda_runtime.h>
 
 #include "sl_device.cuh"
@@ -48,42 +49,100 @@ __device__ __forceinline__ bool fits64(unsigned long long hi, unsigned long long
 
 }  // namespace fx
 
-// RN(a / b) given q0, an estimate of a / b within a few units in its last
-// place (typically RN(a * y) for y ~ 1/b).
-__device__ __forceinline__ double div_from_estimate(double a, double b, double q0)
+// RN(a / b) from an estimate mq * 2^(eq - 1075) of a / b (mq nominally in
+// [2^52, 2^53)).  The rounding decision uses the exact remainder
+// D = ma 2^s - mb mq, which measures a / b - mq in units of mq's last place
+// as D / mb.  FULL = true checks all 128 bits of D and accepts a correction
+// of up to 4 units either way, so any estimate is safe (a poor one only
+// takes the fallback).  FULL = false keeps the low 64 bits of D and is
+// valid only for a LOWER estimate within 1.5 units (0 <= D < 1.5 mb): then
+// the correction is 0 or 1.
+template <bool FULL>
+__device__ __forceinline__ double div_round(double a, double b, unsigned long long mq, int eq)
 {
     using namespace fx;
     const unsigned long long ba = (unsigned long long)__double_as_longlong(a);
     const unsigned long long bb = (unsigned long long)__double_as_longlong(b);
-    const unsigned long long bq = (unsigned long long)__double_as_longlong(q0);
-    const int ea = (int)((ba >> 52) & 0x7ff), eb = (int)((bb >> 52) & 0x7ff), eq = (int)((bq >> 52) & 0x7ff);
+    const int ea = (int)((ba >> 52) & 0x7ff), eb = (int)((bb >> 52) & 0x7ff);
     const unsigned long long sgn = (ba ^ bb) & 0x8000000000000000ull;
     const int s = ea - eb - eq + 1075;
-    bool ok = ea != 0 && ea != 0x7ff && eb != 0 && eb != 0x7ff && eq != 0 && eq != 0x7ff &&
-              ((bq & 0x8000000000000000ull) == sgn) && (s == 52 || s == 53);
-    unsigned long long res = 0;
-    if (ok) {
-        const unsigned long long ma = (ba & kMant) | kHidden, mb = (bb & kMant) | kHidden, mq = (bq & kMant) | kHidden;
-        unsigned long long phi, plo;
-        mul128(mb, mq, phi, plo);
-        const unsigned long long lhi = ma >> (64 - s), llo = ma << s;
-        const unsigned long long dlo = llo - plo;
-        const unsigned long long dhi = lhi - phi - (llo < plo ? 1ull : 0ull);
-        ok = fits64(dhi, dlo);
-        const long long D2 = 2 * (long long)dlo;  // |D| < 2^55 on the fast path
-        const long long m = (long long)mb, m3 = 3 * m, m5 = 5 * m, m7 = 7 * m, m9 = 9 * m;
+    bool ok = ea != 0 && ea != 0x7ff && eb != 0 && eb != 0x7ff && eq >= 1 && eq <= 2046 && (s == 52 || s == 53);
+    const int sh = s == 53 ? 53 : 52;
+    const unsigned long long ma = (ba & kMant) | kHidden, mb = (bb & kMant) | kHidden;
+    const unsigned long long llo = ma << sh, plo = mb * mq;
+    const long long D = (long long)(llo - plo);
+    const long long D2 = 2 * D;
+    const long long m = (long long)mb;
+    int k;
+    if (FULL) {
+        const unsigned long long lhi = ma >> (64 - sh), phi = __umul64hi(mb, mq);
+        ok &= fits64(lhi - phi - (llo < plo ? 1ull : 0ull), llo - plo);
+        ok &= (D < (1ll << 60)) & (D > -(1ll << 60));
+        const long long m3 = 3 * m, m5 = 5 * m, m7 = 7 * m, m9 = 9 * m;
         // k = nearest integer to D/mb, |k| <= 4, as a sum of comparisons
         // (branch-free); ties D2 == odd * mb cannot occur for a quotient of
         // 53-bit numbers but are sent to the fallback all the same
-        const int k = (int)(D2 > m) + (int)(D2 > m3) + (int)(D2 > m5) + (int)(D2 > m7) - (int)(D2 < -m) -
-                      (int)(D2 < -m3) - (int)(D2 < -m5) - (int)(D2 < -m7);
+        k = (int)(D2 > m) + (int)(D2 > m3) + (int)(D2 > m5) + (int)(D2 > m7) - (int)(D2 < -m) - (int)(D2 < -m3) -
+            (int)(D2 < -m5) - (int)(D2 < -m7);
         ok &= (D2 < m9) & (D2 > -m9) & (D2 != m) & (D2 != -m) & (D2 != m3) & (D2 != -m3) & (D2 != m5) &
               (D2 != -m5) & (D2 != m7) & (D2 != -m7);
-        const unsigned long long mr = mq + (long long)k;
-        ok &= mr >= kHidden && mr < (kHidden << 1);
-        res = sgn | ((unsigned long long)eq << 52) | (mr & kMant);
+    } else {
+        k = (int)(D2 > m);
+        ok &= (D2 >= 0) & (D2 < 3 * m) & (D2 != m);
     }
+    const unsigned long long mr = mq + (long long)k;
+    ok &= mr >= kHidden && mr < (kHidden << 1);
+    const unsigned long long res = sgn | ((unsigned long long)eq << 52) | (mr & kMant);
     if (__builtin_expect(!ok, 0)) return a / b;
+    return __longlong_as_double((long long)res);
+}
+
+// RN(a / b) given q0, an estimate of a / b within a few units in its last
+// place (typically RN(a * y) for y ~ 1/b).
+__device__ __forceinline__ double div_from_estimate(double a, double b, double q0)
+{
+    const unsigned long long bq = (unsigned long long)__double_as_longlong(q0);
+    const unsigned long long ba = (unsigned long long)__double_as_longlong(a);
+    const unsigned long long bb = (unsigned long long)__double_as_longlong(b);
+    const int eq = (int)((bq >> 52) & 0x7ff);
+    // a wrong-signed estimate is pushed out of range so that it falls back
+    const bool sign_ok = ((bq ^ ba ^ bb) & 0x8000000000000000ull) == 0;
+    return div_round<true>(a, b, (bq & fx::kMant) | fx::kHidden, sign_ok && eq != 0x7ff ? eq : 0);
+}
+
+// RN(sqrt(x)) from an estimate ms * 2^(es - 1075) (ms nominally in
+// [2^52, 2^53)); x > 0.  All 128 bits of the comparison are checked, so
+// any estimate is safe.
+__device__ __forceinline__ double sqrt_round(double x, unsigned long long ms, int es)
+{
+    using namespace fx;
+    const unsigned long long bx = (unsigned long long)__double_as_longlong(x);
+    const int ex = (int)((bx >> 52) & 0x7ff);
+    const int t = ex - 2 * es + 1075;  // x = mx 2^(ex-1075), estimate = ms 2^(es-1075)
+    bool ok = ex != 0 && ex != 0x7ff && (bx >> 63) == 0 && es >= 1 && es <= 2046 && (t == 52 || t == 53) &&
+              ms < (kHidden << 1);
+    const unsigned long long mx = (bx & kMant) | kHidden;
+    // X4 = mx 2^(t+2): compare with C_j = (2 ms + j)^2 for odd j
+    const int sh = t == 53 ? 55 : 54;
+    const unsigned long long xhi = mx >> (64 - sh), xlo = mx << sh;
+    const unsigned long long two = 2 * ms;  // < 2^54
+    unsigned long long chi, clo;
+    mul128(two, two, chi, clo);            // (2ms)^2
+    // X4 - (2ms)^2 as signed; |.| < 2^62 on the fast path
+    const unsigned long long dlo = xlo - clo;
+    const unsigned long long dhi = xhi - chi - (xlo < clo ? 1ull : 0ull);
+    ok &= fits64(dhi, dlo);
+    const long long E = (long long)dlo;   // X4 - 4 ms^2
+    // C_j - 4 ms^2 = 4 ms j + j^2
+    const long long f = (long long)(2 * two);  // 4 ms  (< 2^55)
+    // sqrt(x) is above ms + j/2 (odd j) iff E > j f + j^2; |k| <= 4
+    const int k = (int)(E > f + 1) + (int)(E > 3 * f + 9) + (int)(E > 5 * f + 25) + (int)(E > 7 * f + 49) -
+                  (int)(E < -f + 1) - (int)(E < -3 * f + 9) - (int)(E < -5 * f + 25) - (int)(E < -7 * f + 49);
+    ok &= (E < 9 * f + 81) & (E > -9 * f + 81);
+    const unsigned long long mr = ms + (long long)k;
+    ok &= mr >= kHidden && mr < (kHidden << 1);
+    const unsigned long long res = ((unsigned long long)es << 52) | (mr & kMant);
+    if (__builtin_expect(!ok, 0)) return sqrt(x);
     return __longlong_as_double((long long)res);
 }
 
@@ -91,39 +150,10 @@ __device__ __forceinline__ double div_from_estimate(double a, double b, double q
 // last place; x > 0.
 __device__ __forceinline__ double sqrt_from_estimate(double x, double s0)
 {
-    using namespace fx;
-    const unsigned long long bx = (unsigned long long)__double_as_longlong(x);
     const unsigned long long bs = (unsigned long long)__double_as_longlong(s0);
-    const int ex = (int)((bx >> 52) & 0x7ff), es = (int)((bs >> 52) & 0x7ff);
-    const int t = ex - 2 * es + 1075;  // x = mx 2^(ex-1075), s0 = ms 2^(es-1075)
-    bool ok = ex != 0 && ex != 0x7ff && es != 0 && es != 0x7ff && (bx >> 63) == 0 && (bs >> 63) == 0 &&
-              (t == 52 || t == 53);
-    unsigned long long res = 0;
-    if (ok) {
-        const unsigned long long mx = (bx & kMant) | kHidden, ms = (bs & kMant) | kHidden;
-        // X4 = mx 2^(t+2): compare with C_j = (2 ms + j)^2 for odd j
-        const int sh = t + 2;  // 54 or 55
-        const unsigned long long xhi = mx >> (64 - sh), xlo = mx << sh;
-        const unsigned long long two = 2 * ms;  // < 2^54
-        unsigned long long chi, clo;
-        mul128(two, two, chi, clo);            // (2ms)^2
-        // X4 - (2ms)^2 as signed; |.| < 2^62 on the fast path
-        const unsigned long long dlo = xlo - clo;
-        const unsigned long long dhi = xhi - chi - (xlo < clo ? 1ull : 0ull);
-        ok = fits64(dhi, dlo);
-        const long long E = (long long)dlo;   // X4 - 4 ms^2
-        // C_j - 4 ms^2 = 4 ms j + j^2
-        const long long f = (long long)(2 * two);  // 4 ms  (< 2^55)
-        // sqrt(x) is above ms + j/2 (odd j) iff E > j f + j^2; |k| <= 4
-        const int k = (int)(E > f + 1) + (int)(E > 3 * f + 9) + (int)(E > 5 * f + 25) + (int)(E > 7 * f + 49) -
-                      (int)(E < -f + 1) - (int)(E < -3 * f + 9) - (int)(E < -5 * f + 25) - (int)(E < -7 * f + 49);
-        ok &= (E < 9 * f + 81) & (E > -9 * f + 81);
-        const unsigned long long mr = ms + (long long)k;
-        ok &= mr >= kHidden && mr < (kHidden << 1);
-        res = ((unsigned long long)es << 52) | (mr & kMant);
-    }
-    if (__builtin_expect(!ok, 0)) return sqrt(x);
-    return __longlong_as_double((long long)res);
+    const int es = (int)((bs >> 52) & 0x7ff);
+    const bool good = (bs >> 63) == 0 && es != 0 && es != 0x7ff;
+    return sqrt_round(x, (bs & fx::kMant) | fx::kHidden, good ? es : 0);
 }
 
 // y / 2 for a normal y by decrementing the exponent (integer pipe)
@@ -145,6 +175,137 @@ __device__ __forceinline__ double rsqrt_refined(double x)
     const double t1 = x * y1;
     const double e1 = fma(-t1, y1, 1.0);
     return fma(half_of(y1), e1, y1);
+}
+
+// ---------------------------------------------------------------------------
+// Estimates on the integer pipe.  A reciprocal significand is held as a
+// 64-bit fixed-point number R ~ 2^116 / mb (mb = the divisor's 53-bit
+// significand), so R is in (2^63, 2^64).  The quotient estimate of a / b is
+// then the high half of (ma 2^11) * R, with no FP64 operation.
+
+// floor((2^116 - 1) / mb) for mb in [2^52, 2^53): restoring division of the
+// all-ones numerator, one quotient bit per step (set-up code only).
+__host__ __device__ inline unsigned long long recip_sig(unsigned long long mb)
+{
+    unsigned long long q = 0, rem = 0;
+    for (int bit = 115; bit >= 0; --bit) {
+        rem = (rem << 1) | 1ull;  // rem < mb < 2^53 before the shift
+        if (rem >= mb) {
+            rem -= mb;
+            if (bit < 64) q |= 1ull << bit;
+        }
+    }
+    return q;
+}
+
+__host__ __device__ inline unsigned long long recip_of(double b)
+{
+    unsigned long long bits;
+    memcpy(&bits, &b, sizeof bits);
+    return recip_sig((bits & fx::kMant) | fx::kHidden);
+}
+
+namespace fx {
+
+// 2 u as a 64-bit fixed-point value, saturating at 2^64 - 1
+__device__ __forceinline__ unsigned long long twice_sat(unsigned long long u)
+{
+    return (u >> 63) ? ~0ull : (u << 1);
+}
+
+// 2^64 * r for a float r in about [0.25, 1]: its 24-bit significand placed
+// by its exponent, saturating at 2^64 - 1
+__device__ __forceinline__ unsigned long long float_to_fix64(float r)
+{
+    const unsigned rb = __float_as_uint(r);
+    const int sh = (int)(rb >> 23) - 86;  // 2^64 r = m24 2^(e - 150 + 64)
+    const unsigned long long m = (rb & 0x7fffffu) | 0x800000u;
+    return sh >= 41 ? ~0ull : (sh < 0 ? 0ull : m << sh);
+}
+
+}  // namespace fx
+
+// R ~ 2^116 / mb for the significand mb of b, to about 2^-60: a 24-bit
+// seed (rcp.approx.ftz.f32 of the top significand bits) and two Newton
+// steps r <- r (2 - g r) in 64-bit fixed point, g = mb / 2^52 in [1, 2).
+__device__ __forceinline__ unsigned long long recip_newton(double b)
+{
+    using namespace fx;
+    const unsigned long long bb = (unsigned long long)__double_as_longlong(b);
+    const unsigned long long mb = (bb & kMant) | kHidden;
+    const float g = __uint_as_float(0x3f800000u | (unsigned)((mb >> 29) & 0x7fffffu));
+    float r0;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r0) : "f"(g));
+    unsigned long long R = float_to_fix64(r0);
+    const unsigned long long G = mb << 11;  // g 2^63
+#pragma unroll
+    for (int it = 0; it < 2; ++it) {
+        const unsigned long long T = __umul64hi(G, R);  // g r 2^63
+        R = twice_sat(__umul64hi(R, 0ull - T));         // r (2 - g r) 2^64
+    }
+    return R;
+}
+
+// RN(a / b) given R ~ 2^116 / mb.  FULL as for div_round: false only for R
+// from recip_sig, whose estimate is a lower one within 1.002 units (R is
+// below 2^116 / mb by less than 1, and each truncation only lowers it);
+// true for R from recip_newton.
+template <bool FULL>
+__device__ __forceinline__ double div_by_fixed(double a, double b, unsigned long long R)
+{
+    using namespace fx;
+    const unsigned long long ba = (unsigned long long)__double_as_longlong(a);
+    const unsigned long long bb = (unsigned long long)__double_as_longlong(b);
+    const int ea = (int)((ba >> 52) & 0x7ff), eb = (int)((bb >> 52) & 0x7ff);
+    const unsigned long long ma = (ba & kMant) | kHidden;
+    const unsigned long long H = __umul64hi(ma << 11, R);  // (ma / mb) 2^63, in (2^62, 2^64)
+    const int c = (int)(H >> 63);
+    return div_round<FULL>(a, b, H >> (10 + c), ea - eb + 1022 + c);
+}
+
+// 1/sqrt(x) for a positive normal x = f 2^(2p), f in [1, 4): returns
+// Y ~ 2^64 / sqrt(f) (to about 2^-60; Y in (2^63, 2^64)) and sets p and
+// F = f 2^62.  A 24-bit seed (rsqrt.approx.ftz.f32 of f's top bits) and two
+// Newton steps y <- y (3 - f y^2) / 2 in 64-bit fixed point.  For other x the
+// outputs are meaningless and the users below fall back.
+__device__ __forceinline__ unsigned long long rsqrt_fix(double x, int& p, unsigned long long& F)
+{
+    using namespace fx;
+    const unsigned long long bx = (unsigned long long)__double_as_longlong(x);
+    const int E = (int)((bx >> 52) & 0x7ff) - 1023;
+    const int odd = E & 1;
+    p = (E - odd) >> 1;
+    const unsigned long long mx = (bx & kMant) | kHidden;
+    F = mx << (10 + odd);
+    const float f = __uint_as_float(((127u + (unsigned)odd) << 23) | (unsigned)((mx >> 29) & 0x7fffffu));
+    float y0;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y0) : "f"(f));
+    unsigned long long Y = float_to_fix64(y0);
+#pragma unroll
+    for (int it = 0; it < 2; ++it) {
+        const unsigned long long S = __umul64hi(Y, Y);     // y^2 2^64
+        const unsigned long long T = __umul64hi(S, F);     // f y^2 2^62
+        Y = twice_sat(__umul64hi(Y, (3ull << 62) - T));    // y (3 - f y^2) 2^63 -> y' 2^64
+    }
+    return Y;
+}
+
+// RN(sqrt(x)) from rsqrt_fix(x): sqrt(f) 2^62 = F Y / 2^64.
+__device__ __forceinline__ double sqrt_fix(double x, unsigned long long F, unsigned long long Y, int p)
+{
+    return sqrt_round(x, __umul64hi(F, Y) >> 10, p + 1023);
+}
+
+// RN(a / d) for d = RN(sqrt(x)), from rsqrt_fix(x) = (Y, p).
+__device__ __forceinline__ double div_by_rsqrt(double a, double d, unsigned long long Y, int p)
+{
+    using namespace fx;
+    const unsigned long long ba = (unsigned long long)__double_as_longlong(a);
+    const int ea = (int)((ba >> 52) & 0x7ff);
+    const unsigned long long ma = (ba & kMant) | kHidden;
+    const unsigned long long H = __umul64hi(ma << 11, Y);  // (ma / sqrt f) 2^11, in (2^62, 2^64)
+    const int c = (int)(H >> 63);
+    return div_round<true>(a, d, H >> (10 + c), ea - p - 1 + c);
 }
 
 }  // namespace sl

@@ -1,5 +1,7 @@
 // sl_kernels.h -- host-side launch interface of the step kernels.
 #pragma once
+#include <cuda.h>
+
 #include "sl_device.cuh"
 
 namespace sl {
@@ -24,8 +26,15 @@ struct StepOverlap {
 };
 
 void launch_derive(const System& s, cudaStream_t st);
+// map: a tensor map of the pair-term buffer (make_pair_map) selects the
+// TMA-streamed row sums; NULL the plain-load form.
 void launch_step(const System& s, bool write, int num_sms, cudaStream_t st, StepTimers* tm,
-                 const StepOverlap* ov = nullptr);
+                 const StepOverlap* ov = nullptr, const CUtensorMap* map = nullptr);
+// Encodes the pair-term buffer's tensor map; false if the driver offers no
+// tensor-map encoder (the plain-load row sums are used then).
+bool make_pair_map(const System& s, CUtensorMap* map);
+// Status bit set by a kernel whose bounded wait for a TMA copy ran out.
+constexpr unsigned kStatusWaitTimeoutBit = 2u;
 void launch_step_mixed(const System& s, bool write, int num_sms, cudaStream_t st, StepTimers* tm);
 void launch_drift(const System& s, cudaStream_t st);
 void launch_energy(const System& s, cudaStream_t st);

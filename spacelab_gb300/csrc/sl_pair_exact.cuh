@@ -4,6 +4,7 @@
 // every file that includes it is compiled with --fmad=false.
 #pragma once
 #include "sl_device.cuh"
+#include "sl_fp64_exact.cuh"
 
 namespace sl {
 
@@ -17,6 +18,32 @@ __device__ __forceinline__ double vdw_coef(double h, double Ra, double Rb, doubl
     const double S = h2 + twoRa * h + twoRb * h;
     const double T = S + fourRa * Rb;
     return cR3a * Rb * Rb * Rb * ((h + Ra + Rb) / (S * S * T * T));
+}
+
+// vdw_coef with the quotient rounded from an integer-pipe reciprocal
+// estimate (sl_fp64_exact.cuh): the same IEEE result.
+__device__ __forceinline__ double vdw_coef_fix(double h, double Ra, double Rb, double twoRa, double twoRb,
+                                               double fourRa, double cR3a)
+{
+    const double h2 = h * h;
+    const double S = h2 + twoRa * h + twoRb * h;
+    const double T = S + fourRa * Rb;
+    const double den = S * S * T * T;
+    return cR3a * Rb * Rb * Rb * div_by_fixed<true>(h + Ra + Rb, den, recip_newton(den));
+}
+
+// vdw_coef_fix for a pair of equal radii R (Ra == Rb bit for bit), with the
+// pair-independent products hoisted: c4 = fourR * R and
+// P = ((cR3 * R) * R) * R.  Every remaining operation is the general
+// form's, in its order, so the result is the same bits.
+__device__ __forceinline__ double vdw_coef_uniform(double h, double R, double twoR, double c4, double P)
+{
+    const double h2 = h * h;
+    const double t = twoR * h;      // twoRa * h == twoRb * h
+    const double S = h2 + t + t;
+    const double T = S + c4;
+    const double den = S * S * T * T;
+    return P * div_by_fixed<true>(h + R + R, den, recip_newton(den));
 }
 
 // U_vdw of ColliderSingleCore.cpp:195-202 / :231-238.

@@ -88,8 +88,10 @@ sl::System static_system(double* base, int n, const sl_material& mat)
     sl::Vec3Soa* vecs[8] = {&s.pos, &s.prev, &s.vel, &s.velh, &s.w, &s.wh, &s.acc, &s.aacc};
     for (int v = 0; v < 8; ++v)
         for (int c = 0; c < 3; ++c) vecs[v]->c[c] = base + kOffVec + (size_t)(3 * v + c) * kVec;
-    double** scal[8] = {&s.R, &s.m, &s.moi, &s.twoR, &s.fourR, &s.cR3, &s.inv_m, &s.inv_moi};
+    double* inv_m_slot = nullptr;  // 8 bytes per sphere, holds the mass reciprocals rm
+    double** scal[8] = {&s.R, &s.m, &s.moi, &s.twoR, &s.fourR, &s.cR3, &inv_m_slot, &s.inv_moi};
     for (int k = 0; k < 8; ++k) *scal[k] = base + kOffScal + (size_t)k * kVec;
+    s.rm = reinterpret_cast<unsigned long long*>(inv_m_slot);
     s.pairbuf = base + kOffPair;
     s.torqbuf = base + kOffTorq;
     s.cmask = reinterpret_cast<uint32_t*>(base + kOffMask);

@@ -1,7 +1,9 @@
 // sl_step.cu -- the FP64 step of SpaceLab's hot path on sm_103a, bit-exact
 // with the reference's sim_one_step (ColliderSingleCore.cpp:78-288).
 //
-// One step is four launches on the handle's stream:
+// One step is four launches on the handle's stream (the row sums have a
+// TMA-streamed form, rowsum_tma_kernel, used whenever a tensor map of the
+// pair-term buffer could be made):
 //   drift_kernel      pass 1 (ColliderSingleCore.cpp:82-97): velh, wh, drift,
 //                     and the previous positions that replace the reference's
 //                     O(N^2) `distances` array (ball_group.hpp:741).
@@ -19,13 +21,19 @@
 // no multiply-add is contracted.  The square root and the quotients of the
 // non-contact path and of the mass divisions are formed as FP64 estimates
 // rounded exactly with integer arithmetic (sl_fp64_exact.cuh): the same
-// IEEE results with most of the work moved off the narrow FP64 pipe.
+// IEEE results with most of the work moved off the narrow FP64 pipe.  The
+// estimates themselves come from the integer pipe too: fixed-point mass
+// reciprocals made once at upload, a fixed-point 1/sqrt(d2) by Newton
+// iteration, and a fixed-point reciprocal of the vdW denominator.
 #include "sl_device.cuh"
 #include "sl_kernels.h"
 #include "sl_fp64_exact.cuh"
 #include "sl_pair_exact.cuh"
+#include "sl_tma.cuh"
 
 #include <cstdio>
+#include <cudaTypedefs.h>
+#include <mutex>
 
 namespace sl {
 
@@ -50,8 +58,8 @@ __global__ void __launch_bounds__(256) drift_kernel(const __grid_constant__ Syst
 // ---------------------------------------------------------------- pass 2 --
 // Per-warp staging of the A block (lane l holds sphere X*32+l).
 struct ABlock {
-    double x[kBlock], y[kBlock], z[kBlock], R[kBlock], twoR[kBlock], fourR[kBlock], cR3[kBlock],
-        m[kBlock], inv_m[kBlock];
+    double x[kBlock], y[kBlock], z[kBlock], R[kBlock], twoR[kBlock], fourR[kBlock], cR3[kBlock], m[kBlock];
+    unsigned long long rm[kBlock];
 };
 
 // One warp per lower-triangular 32x32 block tile (X, Y), X >= Y.  Lane b
@@ -93,13 +101,21 @@ __global__ void __launch_bounds__(128, 3) pair_tile_kernel(const __grid_constant
             const int i = X * kBlock + lane;  // < npad always
             ab.x[lane] = s.pos.c[0][i]; ab.y[lane] = s.pos.c[1][i]; ab.z[lane] = s.pos.c[2][i];
             ab.R[lane] = s.R[i]; ab.twoR[lane] = s.twoR[i]; ab.fourR[lane] = s.fourR[i];
-            ab.cR3[lane] = s.cR3[i]; ab.m[lane] = s.m[i]; ab.inv_m[lane] = s.inv_m[i];
+            ab.cR3[lane] = s.cR3[i]; ab.m[lane] = s.m[i]; ab.rm[lane] = s.rm[i];
         }
         __syncwarp();
         const int B = Y * kBlock + lane;
         const bool bvalid = B < s.n;
         const double bx = s.pos.c[0][B], by = s.pos.c[1][B], bz = s.pos.c[2][B];
-        const double Rb = s.R[B], twoRb = s.twoR[B], mb = s.m[B], inv_mb = s.inv_m[B];
+        const double Rb = s.R[B], twoRb = s.twoR[B], mb = s.m[B];
+        const unsigned long long rmb = s.rm[B];
+        // Equal radii across the tile (monodisperse clusters): the sum of
+        // radii and the vdW coefficient's radius products are the same for
+        // every pair and are formed once.
+        const double R0 = ab.R[0];
+        const bool uni = __all_sync(0xffffffffu, ab.R[lane] == R0 && Rb == R0);
+        const double twoR0 = ab.twoR[0], sum0 = R0 + R0, c40 = ab.fourR[0] * R0;
+        const double P0 = ab.cR3[0] * R0 * R0 * R0;
         const int a_end = min(kBlock, s.n - X * kBlock);
         double pe = 0;
         uint32_t rowbits = 0, colbits = 0;
@@ -112,11 +128,13 @@ __global__ void __launch_bounds__(128, 3) pair_tile_kernel(const __grid_constant
             if (valid) {
                 const int A = X * kBlock + a;
                 const double Ra = ab.R[a];
-                const double sumRaRb = Ra + Rb;                              // :104
+                const double sumRaRb = uni ? sum0 : Ra + Rb;                 // :104
                 const double rx = bx - ab.x[a], ry = by - ab.y[a], rz = bz - ab.z[a];  // :105
                 const double d2 = rx * rx + ry * ry + rz * rz;
-                const double y = rsqrt_refined(d2);                           // ~1/dist
-                const double dist = sqrt_from_estimate(d2, d2 * y);           // :107, RN(sqrt)
+                int p;
+                unsigned long long F;
+                const unsigned long long Y = rsqrt_fix(d2, p, F);             // ~1/sqrt(d2), integer pipe
+                const double dist = sqrt_fix(d2, F, Y, p);                    // :107, RN(sqrt)
                 const double overlap = sumRaRb - dist;                        // :110
                 double fx, fy, fz;
                 if (overlap > 0) {
@@ -139,22 +157,24 @@ __global__ void __launch_bounds__(128, 3) pair_tile_kernel(const __grid_constant
                 } else {
                     double h = fabs(overlap);                                  // :211-215
                     if (h < h_min) h = h_min;
-                    const double coef = vdw_coef(h, Ra, Rb, ab.twoR[a], twoRb, ab.fourR[a], ab.cR3[a]);
-                    fx = coef * div_from_estimate(rx, dist, rx * y);             // :221-227
-                    fy = coef * div_from_estimate(ry, dist, ry * y);
-                    fz = coef * div_from_estimate(rz, dist, rz * y);
+                    const double coef = uni ? vdw_coef_uniform(h, R0, twoR0, c40, P0)
+                                            : vdw_coef_fix(h, Ra, Rb, ab.twoR[a], twoRb, ab.fourR[a], ab.cR3[a]);
+                    fx = coef * div_by_rsqrt(rx, dist, Y, p);                    // :221-227
+                    fy = coef * div_by_rsqrt(ry, dist, Y, p);
+                    fz = coef * div_by_rsqrt(rz, dist, Y, p);
                     if (WRITE) pe += vdw_energy(Ha, h, Ra, Rb, ab.twoR[a]);                    // :239
                 }
                 // :249-250 -- acc[A] += F/m[A]; acc[B] -= F/m[B] (stored negated)
-                const double ma = ab.m[a], ima = ab.inv_m[a];
+                const double ma = ab.m[a];
+                const unsigned long long rma = ab.rm[a];
                 double* pa = rowA + (size_t)a * s.npad;
-                __stcs(pa, div_from_estimate(fx, ma, fx * ima));
-                __stcs(pa + plane, div_from_estimate(fy, ma, fy * ima));
-                __stcs(pa + 2 * plane, div_from_estimate(fz, ma, fz * ima));
+                __stcs(pa, div_by_fixed<false>(fx, ma, rma));
+                __stcs(pa + plane, div_by_fixed<false>(fy, ma, rma));
+                __stcs(pa + 2 * plane, div_by_fixed<false>(fz, ma, rma));
                 double* pb = rowB + a;
-                __stcs(pb, -div_from_estimate(fx, mb, fx * inv_mb));
-                __stcs(pb + plane, -div_from_estimate(fy, mb, fy * inv_mb));
-                __stcs(pb + 2 * plane, -div_from_estimate(fz, mb, fz * inv_mb));
+                __stcs(pb, -div_by_fixed<false>(fx, mb, rmb));
+                __stcs(pb + plane, -div_by_fixed<false>(fy, mb, rmb));
+                __stcs(pb + 2 * plane, -div_by_fixed<false>(fz, mb, rmb));
             }
             const uint32_t bal = __ballot_sync(0xffffffffu, contact);
             if (lane == a) rowbits = bal;
@@ -220,6 +240,109 @@ __global__ void __launch_bounds__(kRowThreads) rowsum_kernel(const __grid_consta
         for (int k = 0; k < kRowBatch; ++k) cur[k] = nxt[k];
     }
     double aacc = first ? 0.0 : s.aacc.c[c][i];
+    const uint32_t* mrow = s.cmask + (size_t)i * s.nb;
+    const double* trow = s.torqbuf + c * plane + (size_t)i * s.npad;
+    for (int Y = b0; Y < b1; ++Y) {
+        uint32_t wd = mrow[Y];
+        while (wd) {
+            const int b = __ffs(wd) - 1;
+            wd &= wd - 1;
+            aacc += trow[Y * kBlock + b];
+        }
+    }
+    s.acc.c[c][i] = acc;
+    s.aacc.c[c][i] = aacc;
+    if (!last) return;
+    const double dt = s.sc->dt;
+    const double v = s.velh.c[c][i] + (.5 * acc) * dt;    // :265
+    const double wv = s.wh.c[c][i] + (.5 * aacc) * dt;    // :266
+    s.vel.c[c][i] = v;
+    s.w.c[c][i] = wv;
+    if (!isfinite(v) || !isfinite(wv) || !isfinite(s.pos.c[c][i])) atomicOr(s.status, 1u);
+}
+
+// ------------------------------------------- row sums, TMA-streamed form --
+// The same sums in the same order as rowsum_kernel, with the pair-term rows
+// streamed into shared memory by TMA: one warp per (component, 32-row
+// block), lane = row.  Stage q of the pipeline holds partner block b0 + q
+// as two 16-column boxes of the warp's 32 rows (8 KB), stored with the
+// 128-byte swizzle so that the lanes' 16-byte reads of their own rows fall
+// in distinct bank groups (4 wavefronts per 512 bytes, the minimum).
+// kRsStages stages are in flight; one lane issues the copies.  A copy that
+// does not land within the bounded wait sets status bit 2 and the warp
+// returns after draining its other copies.
+constexpr int kRsStages = 4;
+constexpr int kRsBox = kBlock * 128;  // one 16-column box of 32 rows
+constexpr int kRsStageBytes = 2 * kRsBox;
+constexpr int kRsSmem = kRsStages * kRsStageBytes + 1024;  // + alignment slack
+
+__device__ __forceinline__ void rs_issue(unsigned char* buf, uint64_t* full, const CUtensorMap* map, int q,
+                                         int Y, int row0)
+{
+    const int st = q % kRsStages;
+    unsigned char* dst = buf + st * kRsStageBytes;
+    tma::mbar_arrive_expect_tx(&full[st], kRsStageBytes);
+    tma::load_2d(dst, map, Y * kBlock, row0, &full[st]);
+    tma::load_2d(dst + kRsBox, map, Y * kBlock + 16, row0, &full[st]);
+}
+
+__global__ void __launch_bounds__(32) rowsum_tma_kernel(const __grid_constant__ System s,
+                                                        const __grid_constant__ CUtensorMap map, int b0, int b1,
+                                                        int first, int last)
+{
+    extern __shared__ unsigned char rs_raw[];
+    __shared__ __align__(8) uint64_t full[kRsStages];
+    unsigned char* buf = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(rs_raw) + 1023) &
+                                                          ~static_cast<uintptr_t>(1023));
+    const int lane = threadIdx.x;
+    const int c = blockIdx.x / s.nb;
+    const int rb = blockIdx.x - c * s.nb;
+    const int i = rb * kBlock + lane;  // < npad
+    const int row0 = c * s.npad + rb * kBlock;
+    const int nq = b1 - b0;
+    const int n = s.n;
+    if (lane == 0) {
+        for (int k = 0; k < kRsStages; ++k) tma::mbar_init(&full[k], 1);
+        tma::fence_barrier_init();
+        for (int q = 0; q < nq && q < kRsStages; ++q) rs_issue(buf, full, &map, q, b0 + q, row0);
+    }
+    __syncwarp();
+
+    double acc = first ? 0.0 : s.acc.c[c][i];
+    int q = 0;
+    bool ok = true;
+    for (; q < nq; ++q) {
+        const int st = q % kRsStages;
+        ok = __all_sync(0xffffffffu, tma::mbar_wait(&full[st], (q / kRsStages) & 1));
+        if (!ok) break;
+        const unsigned char* row = buf + st * kRsStageBytes + lane * 128;
+        const int jb = (b0 + q) * kBlock;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const double2 v = *reinterpret_cast<const double2*>(row + h * kRsBox + ((k ^ (lane & 7)) << 4));
+                const int j = jb + 16 * h + 2 * k;
+                if (j < n && j != i) acc += v.x;
+                if (j + 1 < n && j + 1 != i) acc += v.y;
+            }
+        }
+        __syncwarp();
+        if (lane == 0 && q + kRsStages < nq) {
+            tma::fence_proxy_async();
+            rs_issue(buf, full, &map, q + kRsStages, b0 + q + kRsStages, row0);
+        }
+    }
+    if (!ok) {
+        // drain the copies still in flight (each wait bounded), then report
+        const int issued = min(nq, q + kRsStages);
+        for (int qq = q; qq < issued; ++qq) tma::mbar_wait(&full[qq % kRsStages], (qq / kRsStages) & 1);
+        if (lane == 0) atomicOr(s.status, kStatusWaitTimeoutBit);
+        return;
+    }
+    if (i >= n) return;
+    double aacc = first ? 0.0 : s.aacc.c[c][i];
+    const size_t plane = (size_t)s.npad * s.npad;
     const uint32_t* mrow = s.cmask + (size_t)i * s.nb;
     const double* trow = s.torqbuf + c * plane + (size_t)i * s.npad;
     for (int Y = b0; Y < b1; ++Y) {
@@ -307,7 +430,7 @@ __global__ void derive_kernel(const __grid_constant__ System s)
     s.twoR[i] = 2 * R;
     s.fourR[i] = 4 * R;
     s.cR3[i] = s.mat.Ha / 6 * 64 * R * R * R;
-    s.inv_m[i] = 1.0 / m;
+    s.rm[i] = recip_of(m);
     s.inv_moi[i] = 1.0 / moi;
     if (s.f_R) {  // mixed-precision form: FP32 constants, lengths scaled by 2^-len_shift
         s.f_R[i] = d2f_bits(R, s.len_shift);
@@ -357,6 +480,42 @@ void launch_energy(const System& s, cudaStream_t st)
     energy_final_kernel<<<1, kRedThreads, 0, st>>>(s, nred);
 }
 
+// The pair-term buffer [3][npad][npad] as a 2D FP64 tensor of 3*npad rows
+// of npad columns, boxes of 16 columns x 32 rows with the 128-byte swizzle.
+bool make_pair_map(const System& s, CUtensorMap* map)
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    });
+    if (!encode || !s.pairbuf) return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)s.npad, (cuuint64_t)3 * s.npad};
+    const cuuint64_t strides[1] = {(cuuint64_t)s.npad * sizeof(double)};
+    const cuuint32_t box[2] = {16, (cuuint32_t)kBlock};
+    const cuuint32_t estr[2] = {1, 1};
+    if (encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, s.pairbuf, dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return false;
+    return cudaFuncSetAttribute(rowsum_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kRsSmem) ==
+           cudaSuccess;
+}
+
+static void launch_rowsum(const System& s, cudaStream_t st, const CUtensorMap* map, int b0, int b1, int first,
+                          int last)
+{
+    if (map)
+        rowsum_tma_kernel<<<3 * s.nb, 32, kRsSmem, st>>>(s, *map, b0, b1, first, last);
+    else
+        rowsum_kernel<<<(3 * s.n + kRowThreads - 1) / kRowThreads, kRowThreads, 0, st>>>(s, b0, b1, first, last);
+}
+
 static void launch_pair_columns(const System& s, bool write, int num_sms, cudaStream_t st, int c0, int c1)
 {
     const long long tiles = ((long long)c1 * s.nb - (long long)c1 * (c1 - 1) / 2) -
@@ -368,23 +527,23 @@ static void launch_pair_columns(const System& s, bool write, int num_sms, cudaSt
         pair_tile_kernel<false><<<pb, 128, 0, st>>>(s, c0, c1);
 }
 
-void launch_step(const System& s, bool write, int num_sms, cudaStream_t st, StepTimers* tm, const StepOverlap* ov)
+void launch_step(const System& s, bool write, int num_sms, cudaStream_t st, StepTimers* tm, const StepOverlap* ov,
+                 const CUtensorMap* map)
 {
     launch_drift(s, st);
     if (tm) cudaEventRecord(tm->ev[0], st);
-    const int rb = (3 * s.n + kRowThreads - 1) / kRowThreads;
     int cb[kPairPhases + 1];
     const int np = ov ? phase_bounds(s.nb, cb) : 1;
     if (np <= 1) {
         launch_pair_columns(s, write, num_sms, st, 0, s.nb);
         if (tm) cudaEventRecord(tm->ev[1], st);
-        rowsum_kernel<<<rb, kRowThreads, 0, st>>>(s, 0, s.nb, 1, 1);
+        launch_rowsum(s, st, map, 0, s.nb, 1, 1);
     } else {
         for (int p = 0; p < np; ++p) {
             launch_pair_columns(s, write, num_sms, st, cb[p], cb[p + 1]);
             cudaEventRecord(ov->phase[p], st);
             cudaStreamWaitEvent(ov->side, ov->phase[p], 0);
-            rowsum_kernel<<<rb, kRowThreads, 0, ov->side>>>(s, cb[p], cb[p + 1], p == 0, p == np - 1);
+            launch_rowsum(s, ov->side, map, cb[p], cb[p + 1], p == 0, p == np - 1);
         }
         if (tm) cudaEventRecord(tm->ev[1], st);
         cudaEventRecord(ov->join, ov->side);

@@ -14,7 +14,7 @@ velocities after 100 steps at N=5000 -- is asserted too, as a floor."""
 import numpy as np
 import pytest
 
-from cases import GOLDEN_CASES, GOLDEN_CHECKPOINTS, OracleMaterial, contact_case, material, two_sphere_case
+from cases import DENSITY, GOLDEN_CASES, GOLDEN_CHECKPOINTS, OracleMaterial, contact_case, material, two_sphere_case
 from oracle.oracle import CpuOracle
 from spacelab_gb300 import BallGroup, GpuStep, SpaceLabError, configs
 from spacelab_gb300 import _lib
@@ -111,6 +111,34 @@ def test_exact_matches_oracle_ragged_sizes(n):
                 assert np.array_equal(a[key], b[key]), (n, step, key)
 
 
+@pytest.mark.parametrize("n,odd_every", [(300, 0), (300, 7), (1000, 64)])
+def test_equal_radius_tiles_match_oracle(n, odd_every):
+    """Monodisperse systems take the equal-radius tile form (radius sums and
+    vdW radius products formed once per tile); with a few odd radii some
+    tiles take the general form.  Contacts included; bit-identical."""
+    c = contact_case(n, 2000 + n + odd_every, r_spread=0.0)
+    if odd_every:
+        R = c["R"].copy()
+        R[::odd_every] *= 1.05
+        c["R"] = R
+        c["m"] = DENSITY * 4.0 / 3.0 * np.pi * R ** 3
+        c["moi"] = 0.4 * c["m"] * R * R
+    s, o = _gpu(c), _oracle(c)
+    e0 = o.init()
+    _assert_energy(s.init_conditions(), e0, o.state(), c["m"], c["moi"])
+    assert len(o.contacts()) > 0
+    assert np.array_equal(s.contacts(), o.contacts())
+    for step in range(1, 31):
+        write = step % 10 == 0
+        e = s.sim_one_step(write)
+        eo = o.step(write)
+        if write:
+            _assert_energy(e, eo, o.state(), c["m"], c["moi"])
+    a, b = _state(s), o.state()
+    for key in STATE_KEYS:
+        assert np.array_equal(a[key], b[key]), key
+
+
 def test_two_spheres_touching_and_separated():
     for gap in (-0.05, -1e-9, 0.0, 0.02, 5.0):
         c = two_sphere_case(gap)
@@ -197,6 +225,7 @@ def test_pipelined_step_matches_sequential(n):
     bit for bit and the oracle stays bit-identical."""
     c = contact_case(n, 300 + n)
     a, b = _gpu(c), _gpu(c)
+    a.set_overlap(True)
     b.set_overlap(False)
     o = _oracle(c)
     a.init_conditions(); b.init_conditions(); o.init()
@@ -315,3 +344,43 @@ def test_integer_rounded_quotient_and_sqrt_are_ieee_exact():
     assert np.array_equal(fast_q.view(np.int64), hw_q.view(np.int64))
     assert np.array_equal(hw_s, np.sqrt(np.abs(a)))
     assert np.array_equal(fast_s.view(np.int64), hw_s.view(np.int64))
+
+
+def test_integer_pipe_estimates_round_to_ieee():
+    """The exact step's integer-pipe estimates (fixed-point mass reciprocals,
+    Newton reciprocals, fixed-point 1/sqrt) rounded with the exact remainder
+    equal the IEEE quotient and square root bit for bit."""
+    lib = _lib.lib()
+    rng = np.random.default_rng(11)
+    n = 1 << 21
+    a = rng.normal(0, 1, n) * 10.0 ** rng.uniform(-30, 30, n)
+    b = rng.normal(0, 1, n) * 10.0 ** rng.uniform(-18, 18, n)
+    k = n // 8
+    b[:k] = np.nextafter(2.0 ** rng.integers(-60, 60, k), 0)               # all-ones significands
+    b[k:2 * k] = 2.0 ** rng.integers(-60, 60, k) * (1 + 2.0 ** -52)        # 1 + ulp
+    a[2 * k:3 * k] = b[2 * k:3 * k] * (1 + rng.integers(1, 1 << 20, k) * 2.0 ** -53)  # near midpoints
+    a[3 * k:4 * k] = rng.uniform(1e-6, 3e-3, k)                              # displacements (cm)
+    b[3 * k:4 * k] = rng.uniform(1e-14, 1e-5, k)                             # squared distances
+    a[4 * k:5 * k] = rng.normal(0, 1e-8, k)                                  # forces (dyn)
+    b[4 * k:5 * k] = rng.uniform(1e-12, 6e-11, k)                            # masses (g)
+    a[5 * k:6 * k] = 2.0 ** rng.integers(-100, 100, k)                       # exact powers of two
+    b[5 * k:6 * k] = 2.0 ** rng.integers(-100, 100, k)
+    a[6 * k:6 * k + 8] = [0.0, -0.0, 1.0, -1.0, 2.0 ** -1022, 1e308, 4.0, 9.0]
+    b[6 * k + 8:6 * k + 12] = [2.0 ** -1074, 1e-310, 1.0, 4.0]               # subnormal divisors
+    out = np.zeros(4 * n)
+    assert lib.sl_diag_int_ops(n, _lib.dptr(a), _lib.dptr(b), _lib.dptr(out)) == 0
+    q_set, q_newton, s_fix, q_rsqrt = out.reshape(4, n)
+    with np.errstate(all="ignore"):
+        q = a / b
+        sa = np.sqrt(np.abs(a))
+        qr = a / np.sqrt(np.abs(b))
+
+    def same_bits(got, want):
+        nan = np.isnan(want)  # NaN payloads differ between hosts; NaN must stay NaN
+        assert np.array_equal(np.isnan(got), nan)
+        assert np.array_equal(got[~nan].view(np.int64), want[~nan].view(np.int64))
+
+    same_bits(q_set, q)
+    same_bits(q_newton, q)
+    same_bits(s_fix, sa)
+    same_bits(q_rsqrt, qr)
