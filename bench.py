@@ -231,10 +231,17 @@ def run_ours(args, rank, world, local_rank) -> dict | None:
     contacts = int(len(sim.contacts()))
     pair_ms_avg = pair_ms / launches  # one record per step
     flops_launch = F.pair_flops(w.pairs_per_step, contacts, write=False)
-    peak = _lib.lib()
-    pk = __import__("ctypes").c_double()
-    _lib.check(peak.sl_diag_fp64_peak(__import__("ctypes").byref(pk)), "sl_diag_fp64_peak")
+    import ctypes
+    lib = _lib.lib()
+    pk = ctypes.c_double()
+    _lib.check(lib.sl_diag_fp64_peak(ctypes.byref(pk)), "sl_diag_fp64_peak")
     peak_tflops = pk.value / 1e3
+    # latency of a dependent FP64 add chain (bounds the row sums)
+    chain = {}
+    for wps in (1, 4):
+        cy = ctypes.c_double()
+        _lib.check(lib.sl_diag_fp64_add_latency(wps, 32, ctypes.byref(cy)), "sl_diag_fp64_add_latency")
+        chain[f"{wps}_warps_per_sm"] = cy.value
     achieved_tflops = flops_launch / (pair_ms_avg * 1e-3) / 1e12
     traffic = _read_profile_traffic() if (args.mode == "exact" and w.name == "aggregate_collision_n5000") else None
 
@@ -263,6 +270,7 @@ def run_ours(args, rank, world, local_rank) -> dict | None:
                      "peak_source": "measured live: FP64 FMA chains (sl_diag_fp64_peak), 2 flops per FMA",
                      "flops_per_step": flops_launch, "pair_ms_per_step": pair_ms_avg,
                      "rowsum_exposed_ms_per_step": rowsum_ms / launches,
+                     "fp64_add_chain_cycles": chain,
                      "pair_launches_per_step": pair_launches,
                      "flop_convention": "add/sub/mul/div/sqrt = 1 flop each (spacelab_gb300/flops.py); "
                                         "div and sqrt cost ~7.5 FMA on this GPU",

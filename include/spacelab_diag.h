@@ -21,12 +21,18 @@ int sl_diag_division(int n, const double* a, const double* b, double* q_recip, d
  * IEEE results.  Host arrays; out has 4n entries. */
 int sl_diag_exact_ops(int n, const double* a, const double* b, double* out);
 
-/* The integer-pipe estimates of the exact step, rounded exactly: out[4n]
+/* The integer-pipe arithmetic of the exact step, rounded exactly: out[6n]
  * = a/b with a fixed-point reciprocal of b made at set-up, a/b with a
- * Newton fixed-point reciprocal, sqrt(|a|) from a fixed-point 1/sqrt, and
- * a / RN(sqrt(|b|)) from the fixed-point 1/sqrt of |b|.  Each must equal
- * the IEEE result bit for bit.  No reference counterpart (a self-test). */
+ * Newton fixed-point reciprocal, sqrt(|a|) from a fixed-point 1/sqrt,
+ * a / RN(sqrt(|b|)) from the fixed-point 1/sqrt of |b|, a*b, and -(a/b)
+ * with the sign set in the integer result.  Each must equal the IEEE
+ * result bit for bit.  No reference counterpart (a self-test). */
 int sl_diag_int_ops(int n, const double* a, const double* b, double* out);
+
+/* Latency of a dependent FP64 add chain: one block of warps_per_sm warps per
+ * SM, active_lanes lanes of each warp running a chain; *cycles_per_add at
+ * the rated SM clock.  No reference counterpart (a self-test). */
+int sl_diag_fp64_add_latency(int warps_per_sm, int active_lanes, double* cycles_per_add);
 
 /* Measured FP64 fused-multiply-add throughput of the current GPU in
  * GFLOP/s (2 flops per FMA), from a kernel of independent FMA chains timed

@@ -36,7 +36,8 @@ __global__ void exact_ops_kernel(int n, const double* a, const double* b, double
 // out[0..n): a / b with the fixed-point reciprocal made at set-up
 // (recip_sig), [n..2n): a / b with the Newton reciprocal, [2n..3n):
 // sqrt(|a|) from the fixed-point 1/sqrt, [3n..4n): a / RN(sqrt(|b|)) from
-// the same 1/sqrt of |b|.
+// the same 1/sqrt of |b|, [4n..5n): a * b on the integer pipe, [5n..6n):
+// -(a / b) with the sign set in the integer result.
 __global__ void int_ops_kernel(int n, const double* a, const double* b, const unsigned long long* rb, double* out)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -55,12 +56,29 @@ __global__ void int_ops_kernel(int n, const double* a, const double* b, const un
     const unsigned long long Z = sl::rsqrt_fix(ay, q, G);
     const double d = sl::sqrt_fix(ay, G, Z, q);
     out[3 * (size_t)n + i] = sl::div_by_rsqrt(x, d, Z, q);
+    out[4 * (size_t)n + i] = sl::mul_int(x, y);
+    out[5 * (size_t)n + i] = sl::div_by_fixed<false, true>(x, y, rb[i]);
 }
 
 __global__ void recip_kernel(int n, const double* b, unsigned long long* rb)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) rb[i] = sl::recip_of(b[i]);
+}
+
+// One dependent FP64 add chain per thread of `active` lanes of each warp.
+__global__ void add_chain_kernel(double* out, int iters, int active, double inc)
+{
+    const int lane = threadIdx.x & 31;
+    if (lane >= active) return;
+    double a = threadIdx.x * 1e-3;
+    for (int i = 0; i < iters; ++i) {
+        a = a + inc;
+        a = a + inc;
+        a = a + inc;
+        a = a + inc;
+    }
+    out[blockIdx.x * blockDim.x + threadIdx.x] = a;
 }
 
 constexpr int kChains = 8;
@@ -131,8 +149,8 @@ extern "C" int sl_diag_int_ops(int n, const double* a, const double* b, double* 
     if (n < 1 || !a || !b || !out) return SL_ERR_ARG;
     double* d = nullptr;
     const size_t bytes = (size_t)n * sizeof(double);
-    if (cudaMalloc(&d, 7 * bytes) != cudaSuccess) return SL_ERR_ALLOC;
-    unsigned long long* rb = reinterpret_cast<unsigned long long*>(d + 6 * (size_t)n);
+    if (cudaMalloc(&d, 9 * bytes) != cudaSuccess) return SL_ERR_ALLOC;
+    unsigned long long* rb = reinterpret_cast<unsigned long long*>(d + 8 * (size_t)n);
     int rc = SL_OK;
     if (cudaMemcpy(d, a, bytes, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(d + n, b, bytes, cudaMemcpyHostToDevice) != cudaSuccess)
@@ -142,7 +160,7 @@ extern "C" int sl_diag_int_ops(int n, const double* a, const double* b, double* 
         int_ops_kernel<<<(n + 255) / 256, 256>>>(n, d, d + n, rb, d + 2 * (size_t)n);
         if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) rc = SL_ERR_CUDA;
     }
-    if (rc == SL_OK && cudaMemcpy(out, d + 2 * (size_t)n, 4 * bytes, cudaMemcpyDeviceToHost) != cudaSuccess)
+    if (rc == SL_OK && cudaMemcpy(out, d + 2 * (size_t)n, 6 * bytes, cudaMemcpyDeviceToHost) != cudaSuccess)
         rc = SL_ERR_CUDA;
     cudaFree(d);
     return rc;
@@ -178,5 +196,38 @@ extern "C" int sl_diag_fp64_peak(double* gflops)
     if (rc != SL_OK) return rc;
     const double flops = 2.0 * blocks * threads * (double)kChains * kIters;
     *gflops = flops / (best * 1e-3) / 1e9;
+    return SL_OK;
+}
+
+extern "C" int sl_diag_fp64_add_latency(int warps_per_sm, int active_lanes, double* cycles_per_add)
+{
+    if (warps_per_sm < 1 || warps_per_sm > 32 || active_lanes < 1 || active_lanes > 32 || !cycles_per_add)
+        return SL_ERR_ARG;
+    int dev = 0, sms = 0, khz = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, dev) != cudaSuccess)
+        return SL_ERR_CUDA;
+    const int threads = 32 * warps_per_sm;
+    double* out = nullptr;
+    if (cudaMalloc(&out, (size_t)sms * threads * sizeof(double)) != cudaSuccess) return SL_ERR_ALLOC;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int iters = 20000;
+    add_chain_kernel<<<sms, threads>>>(out, 100, active_lanes, 1e-9);
+    cudaEventRecord(e0);
+    add_chain_kernel<<<sms, threads>>>(out, iters, active_lanes, 1e-9);
+    cudaEventRecord(e1);
+    int rc = SL_OK;
+    if (cudaEventSynchronize(e1) != cudaSuccess || cudaGetLastError() != cudaSuccess) rc = SL_ERR_CUDA;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    if (rc != SL_OK) return rc;
+    // cycles at the device's rated SM clock
+    *cycles_per_add = ms * 1e-3 * (khz * 1e3) / (4.0 * iters);
     return SL_OK;
 }

@@ -30,6 +30,11 @@ namespace sl {
 
 namespace fx {
 
+// The hardware operations of the (rare) fallbacks, kept out of line so that
+// the inlined fast paths stay compact.
+static __device__ __noinline__ double hw_div(double a, double b) { return a / b; }
+static __device__ __noinline__ double hw_sqrt(double x) { return sqrt(x); }
+
 constexpr unsigned long long kMant = 0xfffffffffffffull;
 constexpr unsigned long long kHidden = 1ull << 52;
 
@@ -50,21 +55,22 @@ __device__ __forceinline__ bool fits64(unsigned long long hi, unsigned long long
 }  // namespace fx
 
 // RN(a / b) from an estimate mq * 2^(eq - 1075) of a / b (mq nominally in
-// [2^52, 2^53)).  The rounding decision uses the exact remainder
-// D = ma 2^s - mb mq, which measures a / b - mq in units of mq's last place
-// as D / mb.  FULL = true checks all 128 bits of D and accepts a correction
-// of up to 4 units either way, so any estimate is safe (a poor one only
-// takes the fallback).  FULL = false keeps the low 64 bits of D and is
-// valid only for a LOWER estimate within 1.5 units (0 <= D < 1.5 mb): then
-// the correction is 0 or 1.
-template <bool FULL>
+// [2^52, 2^53)), or its negation -RN(a / b) = RN(-a / b) when NEG.  The
+// rounding decision uses the exact remainder D = ma 2^s - mb mq, which
+// measures a / b - mq in units of mq's last place as D / mb.
+//   FULL = true   checks all 128 bits of D and accepts corrections k of
+//                 -1..2, so any estimate is safe (a poor one only takes the
+//                 fallback); the estimates here are within (-1, 2.1) units.
+//   FULL = false  keeps the low 64 bits of D and is valid only for a LOWER
+//                 estimate within 1.5 units (0 <= D < 1.5 mb): k is 0 or 1.
+template <bool FULL, bool NEG = false>
 __device__ __forceinline__ double div_round(double a, double b, unsigned long long mq, int eq)
 {
     using namespace fx;
     const unsigned long long ba = (unsigned long long)__double_as_longlong(a);
     const unsigned long long bb = (unsigned long long)__double_as_longlong(b);
     const int ea = (int)((ba >> 52) & 0x7ff), eb = (int)((bb >> 52) & 0x7ff);
-    const unsigned long long sgn = (ba ^ bb) & 0x8000000000000000ull;
+    const unsigned long long sgn = ((ba ^ bb) & 0x8000000000000000ull) ^ (NEG ? 0x8000000000000000ull : 0ull);
     const int s = ea - eb - eq + 1075;
     bool ok = ea != 0 && ea != 0x7ff && eb != 0 && eb != 0x7ff && eq >= 1 && eq <= 2046 && (s == 52 || s == 53);
     const int sh = s == 53 ? 53 : 52;
@@ -72,28 +78,25 @@ __device__ __forceinline__ double div_round(double a, double b, unsigned long lo
     const unsigned long long llo = ma << sh, plo = mb * mq;
     const long long D = (long long)(llo - plo);
     const long long D2 = 2 * D;
-    const long long m = (long long)mb;
+    const long long m = (long long)mb, m3 = 3 * m;
     int k;
     if (FULL) {
         const unsigned long long lhi = ma >> (64 - sh), phi = __umul64hi(mb, mq);
         ok &= fits64(lhi - phi - (llo < plo ? 1ull : 0ull), llo - plo);
         ok &= (D < (1ll << 60)) & (D > -(1ll << 60));
-        const long long m3 = 3 * m, m5 = 5 * m, m7 = 7 * m, m9 = 9 * m;
-        // k = nearest integer to D/mb, |k| <= 4, as a sum of comparisons
-        // (branch-free); ties D2 == odd * mb cannot occur for a quotient of
-        // 53-bit numbers but are sent to the fallback all the same
-        k = (int)(D2 > m) + (int)(D2 > m3) + (int)(D2 > m5) + (int)(D2 > m7) - (int)(D2 < -m) - (int)(D2 < -m3) -
-            (int)(D2 < -m5) - (int)(D2 < -m7);
-        ok &= (D2 < m9) & (D2 > -m9) & (D2 != m) & (D2 != -m) & (D2 != m3) & (D2 != -m3) & (D2 != m5) &
-              (D2 != -m5) & (D2 != m7) & (D2 != -m7);
+        // k = nearest integer to D/mb in -1..2 (branch-free); ties
+        // D2 == odd * mb cannot occur for a quotient of 53-bit numbers but
+        // are sent to the fallback all the same
+        k = (int)(D2 > m) + (int)(D2 > m3) - (int)(D2 < -m);
+        ok &= (D2 > -m3) & (D2 < 5 * m) & (D2 != m) & (D2 != -m) & (D2 != m3);
     } else {
         k = (int)(D2 > m);
-        ok &= (D2 >= 0) & (D2 < 3 * m) & (D2 != m);
+        ok &= (D2 >= 0) & (D2 < m3) & (D2 != m);
     }
     const unsigned long long mr = mq + (long long)k;
     ok &= mr >= kHidden && mr < (kHidden << 1);
     const unsigned long long res = sgn | ((unsigned long long)eq << 52) | (mr & kMant);
-    if (__builtin_expect(!ok, 0)) return a / b;
+    if (__builtin_expect(!ok, 0)) return NEG ? -hw_div(a, b) : hw_div(a, b);
     return __longlong_as_double((long long)res);
 }
 
@@ -111,8 +114,9 @@ __device__ __forceinline__ double div_from_estimate(double a, double b, double q
 }
 
 // RN(sqrt(x)) from an estimate ms * 2^(es - 1075) (ms nominally in
-// [2^52, 2^53)); x > 0.  All 128 bits of the comparison are checked, so
-// any estimate is safe.
+// [2^52, 2^53)); x > 0.  All 128 bits of the comparison are checked and
+// corrections of -1..2 units are accepted, so any estimate is safe (a poor
+// one only takes the fallback).
 __device__ __forceinline__ double sqrt_round(double x, unsigned long long ms, int es)
 {
     using namespace fx;
@@ -135,14 +139,14 @@ __device__ __forceinline__ double sqrt_round(double x, unsigned long long ms, in
     const long long E = (long long)dlo;   // X4 - 4 ms^2
     // C_j - 4 ms^2 = 4 ms j + j^2
     const long long f = (long long)(2 * two);  // 4 ms  (< 2^55)
-    // sqrt(x) is above ms + j/2 (odd j) iff E > j f + j^2; |k| <= 4
-    const int k = (int)(E > f + 1) + (int)(E > 3 * f + 9) + (int)(E > 5 * f + 25) + (int)(E > 7 * f + 49) -
-                  (int)(E < -f + 1) - (int)(E < -3 * f + 9) - (int)(E < -5 * f + 25) - (int)(E < -7 * f + 49);
-    ok &= (E < 9 * f + 81) & (E > -9 * f + 81);
+    // sqrt(x) is above ms + j/2 (odd j) iff E > j f + j^2; k in -1..2 (the
+    // estimates here are within (-1, 2) units)
+    const int k = (int)(E > f + 1) + (int)(E > 3 * f + 9) - (int)(E < -f + 1);
+    ok &= (E < 5 * f + 25) & (E > -3 * f + 9);
     const unsigned long long mr = ms + (long long)k;
     ok &= mr >= kHidden && mr < (kHidden << 1);
     const unsigned long long res = ((unsigned long long)es << 52) | (mr & kMant);
-    if (__builtin_expect(!ok, 0)) return sqrt(x);
+    if (__builtin_expect(!ok, 0)) return hw_sqrt(x);
     return __longlong_as_double((long long)res);
 }
 
@@ -246,11 +250,27 @@ __device__ __forceinline__ unsigned long long recip_newton(double b)
     return R;
 }
 
-// RN(a / b) given R ~ 2^116 / mb.  FULL as for div_round: false only for R
-// from recip_sig, whose estimate is a lower one within 1.002 units (R is
-// below 2^116 / mb by less than 1, and each truncation only lowers it);
-// true for R from recip_newton.
-template <bool FULL>
+// div_round<false, NEG> out of line: the near-midpoint quotients of
+// div_by_fixed, about 3 in 1024.
+template <bool NEG>
+__device__ __noinline__ double div_near_mid(double a, double b, unsigned long long mq, int eq)
+{
+    return div_round<false, NEG>(a, b, mq, eq);
+}
+
+// RN(a / b) (or -RN(a / b) when NEG) given R ~ 2^116 / mb.
+//   FULL = true   for R from recip_newton: the estimate goes through
+//                 div_round's 128-bit remainder check.
+//   FULL = false  for R from recip_sig.  Then H = floor(ma 2^11 R / 2^64)
+//                 lies below T = (ma / mb) 2^63 by less than 2.0001 units
+//                 (R is below 2^116 / mb by less than 1 + 2^-52, ma 2^11 <
+//                 2^64, and each truncation only lowers the value).  The
+//                 low bits L of H that the significand drops decide the
+//                 rounding directly unless T's fraction can straddle the
+//                 midpoint, i.e. L is within 2 units below it (about 3 in
+//                 1024 quotients); those take the exact remainder test.
+//                 A quotient of 53-bit numbers is never a midpoint.
+template <bool FULL, bool NEG = false>
 __device__ __forceinline__ double div_by_fixed(double a, double b, unsigned long long R)
 {
     using namespace fx;
@@ -260,7 +280,19 @@ __device__ __forceinline__ double div_by_fixed(double a, double b, unsigned long
     const unsigned long long ma = (ba & kMant) | kHidden;
     const unsigned long long H = __umul64hi(ma << 11, R);  // (ma / mb) 2^63, in (2^62, 2^64)
     const int c = (int)(H >> 63);
-    return div_round<FULL>(a, b, H >> (10 + c), ea - eb + 1022 + c);
+    const unsigned long long mq = H >> (10 + c);
+    const int eq = ea - eb + 1022 + c;
+    if (FULL) return div_round<true, NEG>(a, b, mq, eq);
+    const unsigned L = (unsigned)H & ((2u << (9 + c)) - 1u);  // dropped bits
+    const unsigned half = 1u << (9 + c);
+    if (__builtin_expect(L + 2u >= half && L <= half, 0)) return div_near_mid<NEG>(a, b, mq, eq);
+    const unsigned long long mr = mq + (L > half ? 1ull : 0ull);
+    const bool ok = ea != 0 && ea != 0x7ff && eb != 0 && eb != 0x7ff && eq >= 1 && eq <= 2045 && mr >= kHidden;
+    const unsigned long long sgn = ((ba ^ bb) & 0x8000000000000000ull) ^ (NEG ? 0x8000000000000000ull : 0ull);
+    // mr == 2^53 carries into the exponent field, which is the right result
+    const unsigned long long res = sgn | (((unsigned long long)eq << 52) + (mr - kHidden));
+    if (__builtin_expect(!ok, 0)) return NEG ? -fx::hw_div(a, b) : fx::hw_div(a, b);
+    return __longlong_as_double((long long)res);
 }
 
 // 1/sqrt(x) for a positive normal x = f 2^(2p), f in [1, 4): returns
@@ -306,6 +338,35 @@ __device__ __forceinline__ double div_by_rsqrt(double a, double d, unsigned long
     const unsigned long long H = __umul64hi(ma << 11, Y);  // (ma / sqrt f) 2^11, in (2^62, 2^64)
     const int c = (int)(H >> 63);
     return div_round<true>(a, d, H >> (10 + c), ea - p - 1 + c);
+}
+
+// RN(a * b) on the integer pipe: the 106-bit product of the significands
+// from one 64x64 high product H = floor(ma mb 2^22 / 2^64) and the low 64
+// bits Lo, which together hold it exactly; the bits H drops below the
+// 53-bit significand (L) and Lo != 0 (sticky) decide round-to-nearest-even.
+// Zero, subnormal, Inf/NaN operands and results outside the normal range
+// take the hardware multiply.
+__device__ __forceinline__ double mul_int(double a, double b)
+{
+    using namespace fx;
+    const unsigned long long ba = (unsigned long long)__double_as_longlong(a);
+    const unsigned long long bb = (unsigned long long)__double_as_longlong(b);
+    const int ea = (int)((ba >> 52) & 0x7ff), eb = (int)((bb >> 52) & 0x7ff);
+    const unsigned long long x = ((ba & kMant) | kHidden) << 11, y = ((bb & kMant) | kHidden) << 11;
+    const unsigned long long H = __umul64hi(x, y);  // in [2^62, 2^64)
+    const unsigned long long Lo = x * y;
+    const int c = (int)(H >> 63);
+    const unsigned long long mq = H >> (10 + c);
+    const unsigned L = (unsigned)H & ((2u << (9 + c)) - 1u);
+    const unsigned half = 1u << (9 + c);
+    const bool up = L > half || (L == half && (Lo != 0ull || (mq & 1ull)));
+    const int e = ea + eb - 1023 + c;
+    const bool ok = ea != 0 && ea != 0x7ff && eb != 0 && eb != 0x7ff && e >= 1 && e <= 2045;
+    const unsigned long long sgn = (ba ^ bb) & 0x8000000000000000ull;
+    // mq + up == 2^53 carries into the exponent field, which is the right result
+    const unsigned long long res = sgn | (((unsigned long long)e << 52) + (mq + (up ? 1ull : 0ull) - kHidden));
+    if (__builtin_expect(!ok, 0)) return a * b;
+    return __longlong_as_double((long long)res);
 }
 
 }  // namespace sl

@@ -62,6 +62,89 @@ struct ABlock {
     unsigned long long rm[kBlock];
 };
 
+// Equal radii across a tile (monodisperse clusters): the sum of radii and
+// the vdW coefficient's radius products are the same for every pair of the
+// tile and are formed once (vdw_coef_uniform).
+struct TileUniform {
+    double R0, twoR0, sum0, c40, P0;
+};
+
+// The pairs of one tile (X, Y) for lane = sphere B: terms to pairbuf and
+// torqbuf, contact bits to rowbits/colbits, PE (write steps) to pe.
+template <bool WRITE, bool UNI>
+__device__ __forceinline__ void tile_pairs(const System& s, const ABlock& ab, int X, int Y, int lane, int a_end,
+                                           double bx, double by, double bz, double Rb, double twoRb, double mb,
+                                           unsigned long long rmb, bool bvalid, const TileUniform& tu,
+                                           long long h_min_bits, double Ha, double* rowA, double* rowB,
+                                           double& pe, uint32_t& rowbits, uint32_t& colbits)
+{
+    const size_t plane = (size_t)s.npad * s.npad;
+    const int B = Y * kBlock + lane;
+    for (int a = 0; a < a_end; ++a) {
+        const bool valid = bvalid && (X != Y || lane < a);
+        bool contact = false;
+        if (valid) {
+            const int A = X * kBlock + a;
+            const double Ra = ab.R[a];
+            const double sumRaRb = UNI ? tu.sum0 : Ra + Rb;              // :104
+            const double rx = bx - ab.x[a], ry = by - ab.y[a], rz = bz - ab.z[a];  // :105
+            const double d2 = rx * rx + ry * ry + rz * rz;
+            int p;
+            unsigned long long F;
+            const unsigned long long Yr = rsqrt_fix(d2, p, F);            // ~1/sqrt(d2), integer pipe
+            const double dist = sqrt_fix(d2, F, Yr, p);                   // :107, RN(sqrt)
+            const double overlap = sumRaRb - dist;                        // :110
+            // the comparisons of the step are made on the bit patterns
+            // (integer pipe): for doubles of one sign the integer order
+            // is the FP order; NaN is excluded explicitly
+            const long long ob = __double_as_longlong(overlap);
+            double fx, fy, fz;
+            if (ob > 0 && ob <= 0x7ff0000000000000ll) {                    // overlap > 0
+                contact = true;
+                const ContactIn in = gather_contact(s, A, B);
+                const ContactOut o = contact_pair_exact<WRITE>(in, s.mat, rx, ry, rz, dist, overlap, Ra, Rb,
+                                                               ab.twoR[a], twoRb, ab.fourR[a], ab.cR3[a]);
+                fx = o.fx; fy = o.fy; fz = o.fz;
+                const double im_a = s.inv_moi[A], mo_a = s.moi[A];
+                const double im_b = s.inv_moi[B], mo_b = s.moi[B];
+                double* ta = s.torqbuf + (size_t)A * s.npad + B;   // :187
+                double* tb = s.torqbuf + (size_t)B * s.npad + A;   // :188
+                ta[0] = div_by_recip(o.tax, mo_a, im_a);
+                ta[plane] = div_by_recip(o.tay, mo_a, im_a);
+                ta[2 * plane] = div_by_recip(o.taz, mo_a, im_a);
+                tb[0] = div_by_recip(o.tbx, mo_b, im_b);
+                tb[plane] = div_by_recip(o.tby, mo_b, im_b);
+                tb[2 * plane] = div_by_recip(o.tbz, mo_b, im_b);
+                if (WRITE) pe += o.pe;
+            } else {
+                long long hb = ob & 0x7fffffffffffffffll;                  // :211-215 |overlap|
+                if (hb < h_min_bits) hb = h_min_bits;                      // h < h_min (NaN stays NaN)
+                const double h = __longlong_as_double(hb);
+                const double coef = UNI ? vdw_coef_uniform(h, tu.R0, tu.twoR0, tu.c40, tu.P0)
+                                        : vdw_coef_fix(h, Ra, Rb, ab.twoR[a], twoRb, ab.fourR[a], ab.cR3[a]);
+                fx = coef * div_by_rsqrt(rx, dist, Yr, p);                    // :221-227
+                fy = coef * div_by_rsqrt(ry, dist, Yr, p);
+                fz = coef * div_by_rsqrt(rz, dist, Yr, p);
+                if (WRITE) pe += vdw_energy(Ha, h, Ra, Rb, ab.twoR[a]);                    // :239
+            }
+            // :249-250 -- acc[A] += F/m[A]; acc[B] -= F/m[B] (stored negated)
+            const double ma = ab.m[a];
+            const unsigned long long rma = ab.rm[a];
+            double* pa = rowA + (size_t)a * s.npad;
+            __stcs(pa, div_by_fixed<false>(fx, ma, rma));
+            __stcs(pa + plane, div_by_fixed<false>(fy, ma, rma));
+            __stcs(pa + 2 * plane, div_by_fixed<false>(fz, ma, rma));
+            double* pb = rowB + a;
+            __stcs(pb, div_by_fixed<false, true>(fx, mb, rmb));  // -(F/m[B]), sign set in the integer result
+            __stcs(pb + plane, div_by_fixed<false, true>(fy, mb, rmb));
+            __stcs(pb + 2 * plane, div_by_fixed<false, true>(fz, mb, rmb));
+        }
+        const uint32_t bal = __ballot_sync(0xffffffffu, contact);
+        if (lane == a) rowbits = bal;
+        if (contact) colbits |= 1u << a;
+    }
+}
+
 // One warp per lower-triangular 32x32 block tile (X, Y), X >= Y.  Lane b
 // owns sphere B = 32Y + b and walks the 32 spheres A = 32X + a of the A
 // block; on the diagonal only a > b is a pair.  Tiles are independent; one
@@ -89,8 +172,8 @@ __global__ void __launch_bounds__(128, 3) pair_tile_kernel(const __grid_constant
     const int wib = threadIdx.x >> 5;
     ABlock& ab = sA[wib];
     const long long nwarps = (long long)gridDim.x * 4;
-    const size_t plane = (size_t)s.npad * s.npad;
-    const double Ha = s.mat.Ha, h_min = s.mat.h_min;
+    const double Ha = s.mat.Ha;
+    const long long h_min_bits = __double_as_longlong(s.mat.h_min);  // h_min > 0
 
     const long long u1 = col_offset(s.nb, c1);
     for (long long u = col_offset(s.nb, c0) + (long long)blockIdx.x * 4 + wib; u < u1; u += nwarps) {
@@ -109,9 +192,6 @@ __global__ void __launch_bounds__(128, 3) pair_tile_kernel(const __grid_constant
         const double bx = s.pos.c[0][B], by = s.pos.c[1][B], bz = s.pos.c[2][B];
         const double Rb = s.R[B], twoRb = s.twoR[B], mb = s.m[B];
         const unsigned long long rmb = s.rm[B];
-        // Equal radii across the tile (monodisperse clusters): the sum of
-        // radii and the vdW coefficient's radius products are the same for
-        // every pair and are formed once.
         const double R0 = ab.R[0];
         const bool uni = __all_sync(0xffffffffu, ab.R[lane] == R0 && Rb == R0);
         const double twoR0 = ab.twoR[0], sum0 = R0 + R0, c40 = ab.fourR[0] * R0;
@@ -122,64 +202,13 @@ __global__ void __launch_bounds__(128, 3) pair_tile_kernel(const __grid_constant
         double* rowA = s.pairbuf + (size_t)(X * kBlock) * s.npad + B;  // + a*npad: term for A
         double* rowB = s.pairbuf + (size_t)B * s.npad + X * kBlock;    // + a: term for B
 
-        for (int a = 0; a < a_end; ++a) {
-            const bool valid = bvalid && (X != Y || lane < a);
-            bool contact = false;
-            if (valid) {
-                const int A = X * kBlock + a;
-                const double Ra = ab.R[a];
-                const double sumRaRb = uni ? sum0 : Ra + Rb;                 // :104
-                const double rx = bx - ab.x[a], ry = by - ab.y[a], rz = bz - ab.z[a];  // :105
-                const double d2 = rx * rx + ry * ry + rz * rz;
-                int p;
-                unsigned long long F;
-                const unsigned long long Y = rsqrt_fix(d2, p, F);             // ~1/sqrt(d2), integer pipe
-                const double dist = sqrt_fix(d2, F, Y, p);                    // :107, RN(sqrt)
-                const double overlap = sumRaRb - dist;                        // :110
-                double fx, fy, fz;
-                if (overlap > 0) {
-                    contact = true;
-                    const ContactIn in = gather_contact(s, A, B);
-                    const ContactOut o = contact_pair_exact<WRITE>(in, s.mat, rx, ry, rz, dist, overlap, Ra, Rb,
-                                                                   ab.twoR[a], twoRb, ab.fourR[a], ab.cR3[a]);
-                    fx = o.fx; fy = o.fy; fz = o.fz;
-                    const double im_a = s.inv_moi[A], mo_a = s.moi[A];
-                    const double im_b = s.inv_moi[B], mo_b = s.moi[B];
-                    double* ta = s.torqbuf + (size_t)A * s.npad + B;   // :187
-                    double* tb = s.torqbuf + (size_t)B * s.npad + A;   // :188
-                    ta[0] = div_by_recip(o.tax, mo_a, im_a);
-                    ta[plane] = div_by_recip(o.tay, mo_a, im_a);
-                    ta[2 * plane] = div_by_recip(o.taz, mo_a, im_a);
-                    tb[0] = div_by_recip(o.tbx, mo_b, im_b);
-                    tb[plane] = div_by_recip(o.tby, mo_b, im_b);
-                    tb[2 * plane] = div_by_recip(o.tbz, mo_b, im_b);
-                    if (WRITE) pe += o.pe;
-                } else {
-                    double h = fabs(overlap);                                  // :211-215
-                    if (h < h_min) h = h_min;
-                    const double coef = uni ? vdw_coef_uniform(h, R0, twoR0, c40, P0)
-                                            : vdw_coef_fix(h, Ra, Rb, ab.twoR[a], twoRb, ab.fourR[a], ab.cR3[a]);
-                    fx = coef * div_by_rsqrt(rx, dist, Y, p);                    // :221-227
-                    fy = coef * div_by_rsqrt(ry, dist, Y, p);
-                    fz = coef * div_by_rsqrt(rz, dist, Y, p);
-                    if (WRITE) pe += vdw_energy(Ha, h, Ra, Rb, ab.twoR[a]);                    // :239
-                }
-                // :249-250 -- acc[A] += F/m[A]; acc[B] -= F/m[B] (stored negated)
-                const double ma = ab.m[a];
-                const unsigned long long rma = ab.rm[a];
-                double* pa = rowA + (size_t)a * s.npad;
-                __stcs(pa, div_by_fixed<false>(fx, ma, rma));
-                __stcs(pa + plane, div_by_fixed<false>(fy, ma, rma));
-                __stcs(pa + 2 * plane, div_by_fixed<false>(fz, ma, rma));
-                double* pb = rowB + a;
-                __stcs(pb, -div_by_fixed<false>(fx, mb, rmb));
-                __stcs(pb + plane, -div_by_fixed<false>(fy, mb, rmb));
-                __stcs(pb + 2 * plane, -div_by_fixed<false>(fz, mb, rmb));
-            }
-            const uint32_t bal = __ballot_sync(0xffffffffu, contact);
-            if (lane == a) rowbits = bal;
-            if (contact) colbits |= 1u << a;
-        }
+        const TileUniform tu{R0, twoR0, sum0, c40, P0};
+        if (uni)
+            tile_pairs<WRITE, true>(s, ab, X, Y, lane, a_end, bx, by, bz, Rb, twoRb, mb, rmb, bvalid, tu, h_min_bits,
+                                    Ha, rowA, rowB, pe, rowbits, colbits);
+        else
+            tile_pairs<WRITE, false>(s, ab, X, Y, lane, a_end, bx, by, bz, Rb, twoRb, mb, rmb, bvalid, tu, h_min_bits,
+                                     Ha, rowA, rowB, pe, rowbits, colbits);
         // Contact bits: row A = 32X + lane gets block Y's bits, row B gets
         // block X's bits; on the diagonal both describe row 32X + lane.
         if (X == Y) {
@@ -262,19 +291,24 @@ __global__ void __launch_bounds__(kRowThreads) rowsum_kernel(const __grid_consta
 }
 
 // ------------------------------------------- row sums, TMA-streamed form --
-// The same sums in the same order as rowsum_kernel, with the pair-term rows
-// streamed into shared memory by TMA: one warp per (component, 32-row
-// block), lane = row.  Stage q of the pipeline holds partner block b0 + q
+// The same sums in the same order as rowsum_kernel, for a handle's own
+// arena (whose never-written pair-term entries are +0.0), with the
+// pair-term rows streamed into shared memory by TMA: one warp per
+// (component, 32-row block), lane = row, kRsWarps independent warps per CTA
+// so that the warps (and their FP64 add chains) spread over the SM's four
+// sub-partitions.  Stage q of the pipeline holds partner block b0 + q
 // as two 16-column boxes of the warp's 32 rows (8 KB), stored with the
 // 128-byte swizzle so that the lanes' 16-byte reads of their own rows fall
 // in distinct bank groups (4 wavefronts per 512 bytes, the minimum).
 // kRsStages stages are in flight; one lane issues the copies.  A copy that
 // does not land within the bounded wait sets status bit 2 and the warp
 // returns after draining its other copies.
-constexpr int kRsStages = 4;
+constexpr int kRsStages = 3;
+constexpr int kRsWarps = 2;  // independent warps per CTA (each on its own SM sub-partition)
 constexpr int kRsBox = kBlock * 128;  // one 16-column box of 32 rows
 constexpr int kRsStageBytes = 2 * kRsBox;
-constexpr int kRsSmem = kRsStages * kRsStageBytes + 1024;  // + alignment slack
+constexpr int kRsWarpBytes = kRsStages * kRsStageBytes;
+constexpr int kRsSmem = kRsWarps * kRsWarpBytes + 1024;  // + alignment slack
 
 __device__ __forceinline__ void rs_issue(unsigned char* buf, uint64_t* full, const CUtensorMap* map, int q,
                                          int Y, int row0)
@@ -286,17 +320,22 @@ __device__ __forceinline__ void rs_issue(unsigned char* buf, uint64_t* full, con
     tma::load_2d(dst + kRsBox, map, Y * kBlock + 16, row0, &full[st]);
 }
 
-__global__ void __launch_bounds__(32) rowsum_tma_kernel(const __grid_constant__ System s,
-                                                        const __grid_constant__ CUtensorMap map, int b0, int b1,
-                                                        int first, int last)
+__global__ void __launch_bounds__(32 * kRsWarps) rowsum_tma_kernel(const __grid_constant__ System s,
+                                                                   const __grid_constant__ CUtensorMap map, int b0,
+                                                                   int b1, int first, int last)
 {
     extern __shared__ unsigned char rs_raw[];
-    __shared__ __align__(8) uint64_t full[kRsStages];
+    __shared__ __align__(8) uint64_t full_all[kRsWarps][kRsStages];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int wg = blockIdx.x * kRsWarps + warp;  // global (component, row block) index
+    if (wg >= 3 * s.nb) return;                   // no block-wide synchronisation below
     unsigned char* buf = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(rs_raw) + 1023) &
-                                                          ~static_cast<uintptr_t>(1023));
-    const int lane = threadIdx.x;
-    const int c = blockIdx.x / s.nb;
-    const int rb = blockIdx.x - c * s.nb;
+                                                          ~static_cast<uintptr_t>(1023)) +
+                         warp * kRsWarpBytes;
+    uint64_t* full = full_all[warp];
+    const int c = wg / s.nb;
+    const int rb = wg - c * s.nb;
     const int i = rb * kBlock + lane;  // < npad
     const int row0 = c * s.npad + rb * kBlock;
     const int nq = b1 - b0;
@@ -308,51 +347,72 @@ __global__ void __launch_bounds__(32) rowsum_tma_kernel(const __grid_constant__ 
     }
     __syncwarp();
 
+    // Software pipeline: stage q's 32 values are in registers (cur) while
+    // its buffer is already refilled and stage q+1 is read; the dependent
+    // add chain thus never waits for shared memory.
     double acc = first ? 0.0 : s.acc.c[c][i];
+    double aacc = first ? 0.0 : s.aacc.c[c][i];
+    // torque terms: contact partners only, in the same ascending order; the
+    // contact-mask word of the next partner block is loaded a stage ahead
+    const size_t plane = (size_t)s.npad * s.npad;
+    const uint32_t* mrow = s.cmask + (size_t)i * s.nb;  // rows < npad exist; padding rows are 0
+    const double* trow = s.torqbuf + c * plane + (size_t)i * s.npad;
+    uint32_t wnext = nq > 0 ? mrow[b0] : 0u;
+    double2 cur[16], nxt[16];
+    bool ok = nq <= 0 || __all_sync(0xffffffffu, tma::mbar_wait(&full[0], 0));
+    if (ok && nq > 0) {
+#pragma unroll
+        for (int k = 0; k < 16; ++k)
+            cur[k] = *reinterpret_cast<const double2*>(buf + lane * 128 + (k >> 3) * kRsBox + (((k & 7) ^ (lane & 7)) << 4));
+    }
     int q = 0;
-    bool ok = true;
-    for (; q < nq; ++q) {
-        const int st = q % kRsStages;
-        ok = __all_sync(0xffffffffu, tma::mbar_wait(&full[st], (q / kRsStages) & 1));
-        if (!ok) break;
-        const unsigned char* row = buf + st * kRsStageBytes + lane * 128;
-        const int jb = (b0 + q) * kBlock;
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-#pragma unroll
-            for (int k = 0; k < 8; ++k) {
-                const double2 v = *reinterpret_cast<const double2*>(row + h * kRsBox + ((k ^ (lane & 7)) << 4));
-                const int j = jb + 16 * h + 2 * k;
-                if (j < n && j != i) acc += v.x;
-                if (j + 1 < n && j + 1 != i) acc += v.y;
-            }
-        }
-        __syncwarp();
+    for (; ok && q < nq; ++q) {
+        __syncwarp();  // every lane has stage q in registers: its buffer is free
         if (lane == 0 && q + kRsStages < nq) {
             tma::fence_proxy_async();
             rs_issue(buf, full, &map, q + kRsStages, b0 + q + kRsStages, row0);
         }
+        if (q + 1 < nq) {
+            const int st1 = (q + 1) % kRsStages;
+            ok = __all_sync(0xffffffffu, tma::mbar_wait(&full[st1], ((q + 1) / kRsStages) & 1));
+            if (ok) {
+                const unsigned char* row = buf + st1 * kRsStageBytes + lane * 128;
+#pragma unroll
+                for (int k = 0; k < 16; ++k)
+                    nxt[k] = *reinterpret_cast<const double2*>(row + (k >> 3) * kRsBox + (((k & 7) ^ (lane & 7)) << 4));
+            }
+        }
+        // Every entry is added, the row's own column and the padding columns
+        // included: those are never written and hold +0.0 (the arena is
+        // zeroed at creation and n is fixed per handle), and adding +0.0
+        // leaves the sum unchanged -- a sum of RN additions that starts at
+        // +0.0 is never -0.0.  The chain is then DADDs only.
+        const int jb = (b0 + q) * kBlock;
+        uint32_t wd = wnext;
+        if (q + 1 < nq) wnext = mrow[b0 + q + 1];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            acc += cur[k].x;
+            acc += cur[k].y;
+        }
+        while (wd) {
+            const int bit = __ffs(wd) - 1;
+            wd &= wd - 1;
+            aacc += trow[jb + bit];
+        }
+#pragma unroll
+        for (int k = 0; k < 16; ++k) cur[k] = nxt[k];
     }
+    // on a failed wait q is the first stage not observed complete
     if (!ok) {
-        // drain the copies still in flight (each wait bounded), then report
+        // drain the copies still in flight (each wait bounded), then report;
+        // stages q .. q + kRsStages - 1 may have been issued
         const int issued = min(nq, q + kRsStages);
         for (int qq = q; qq < issued; ++qq) tma::mbar_wait(&full[qq % kRsStages], (qq / kRsStages) & 1);
         if (lane == 0) atomicOr(s.status, kStatusWaitTimeoutBit);
         return;
     }
     if (i >= n) return;
-    double aacc = first ? 0.0 : s.aacc.c[c][i];
-    const size_t plane = (size_t)s.npad * s.npad;
-    const uint32_t* mrow = s.cmask + (size_t)i * s.nb;
-    const double* trow = s.torqbuf + c * plane + (size_t)i * s.npad;
-    for (int Y = b0; Y < b1; ++Y) {
-        uint32_t wd = mrow[Y];
-        while (wd) {
-            const int b = __ffs(wd) - 1;
-            wd &= wd - 1;
-            aacc += trow[Y * kBlock + b];
-        }
-    }
     s.acc.c[c][i] = acc;
     s.aacc.c[c][i] = aacc;
     if (!last) return;
@@ -511,7 +571,8 @@ static void launch_rowsum(const System& s, cudaStream_t st, const CUtensorMap* m
                           int last)
 {
     if (map)
-        rowsum_tma_kernel<<<3 * s.nb, 32, kRsSmem, st>>>(s, *map, b0, b1, first, last);
+        rowsum_tma_kernel<<<(3 * s.nb + kRsWarps - 1) / kRsWarps, 32 * kRsWarps, kRsSmem, st>>>(s, *map, b0, b1,
+                                                                                            first, last);
     else
         rowsum_kernel<<<(3 * s.n + kRowThreads - 1) / kRowThreads, kRowThreads, 0, st>>>(s, b0, b1, first, last);
 }

@@ -347,9 +347,9 @@ def test_integer_rounded_quotient_and_sqrt_are_ieee_exact():
 
 
 def test_integer_pipe_estimates_round_to_ieee():
-    """The exact step's integer-pipe estimates (fixed-point mass reciprocals,
-    Newton reciprocals, fixed-point 1/sqrt) rounded with the exact remainder
-    equal the IEEE quotient and square root bit for bit."""
+    """The exact step's integer-pipe arithmetic (fixed-point mass
+    reciprocals, Newton reciprocals, fixed-point 1/sqrt, products) equals
+    the IEEE quotient, square root and product bit for bit."""
     lib = _lib.lib()
     rng = np.random.default_rng(11)
     n = 1 << 21
@@ -367,13 +367,16 @@ def test_integer_pipe_estimates_round_to_ieee():
     b[5 * k:6 * k] = 2.0 ** rng.integers(-100, 100, k)
     a[6 * k:6 * k + 8] = [0.0, -0.0, 1.0, -1.0, 2.0 ** -1022, 1e308, 4.0, 9.0]
     b[6 * k + 8:6 * k + 12] = [2.0 ** -1074, 1e-310, 1.0, 4.0]               # subnormal divisors
-    out = np.zeros(4 * n)
+    a[7 * k:7 * k + k // 2] = 3.0 * 2.0 ** rng.integers(-40, 40, k // 2)      # exact product ties
+    b[7 * k:7 * k + k // 2] = 1.0 + (2 * rng.integers(0, 1 << 40, k // 2) + 1) * 2.0 ** -52
+    out = np.zeros(6 * n)
     assert lib.sl_diag_int_ops(n, _lib.dptr(a), _lib.dptr(b), _lib.dptr(out)) == 0
-    q_set, q_newton, s_fix, q_rsqrt = out.reshape(4, n)
+    q_set, q_newton, s_fix, q_rsqrt, prod, q_neg = out.reshape(6, n)
     with np.errstate(all="ignore"):
         q = a / b
         sa = np.sqrt(np.abs(a))
         qr = a / np.sqrt(np.abs(b))
+        ab = a * b
 
     def same_bits(got, want):
         nan = np.isnan(want)  # NaN payloads differ between hosts; NaN must stay NaN
@@ -384,3 +387,5 @@ def test_integer_pipe_estimates_round_to_ieee():
     same_bits(q_newton, q)
     same_bits(s_fix, sa)
     same_bits(q_rsqrt, qr)
+    same_bits(prod, ab)
+    same_bits(q_neg, -q)
