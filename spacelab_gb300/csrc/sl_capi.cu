@@ -3,9 +3,9 @@
 // A handle owns one device arena holding the structure-of-arrays state of
 // one system, the per-pair scratch (pairbuf/torqbuf/cmask) and the energy
 // reduction buffers, plus a CUDA stream and, for sl_run, an instantiated
-// CUDA graph of one write interval.  All host<->device copies go through a
-// pinned staging buffer that also performs the AoS (vec3[n]) <-> SoA
-// transposition.
+// CUDA graph of one write interval.  The caller's vec3[n] (AoS) arrays are
+// copied as they are, one copy per array, into a device staging area, and a
+// kernel transposes them to or from the SoA state.
 #include "../../include/spacelab_gpu.h"
 #include "sl_device.cuh"
 #include "sl_kernels.h"
@@ -67,7 +67,8 @@ struct sl_handle {
     bool overlap = false;  // steps use them
     void* arena = nullptr;
     size_t arena_bytes = 0;
-    double* staging = nullptr;  // pinned, 18 * npad doubles
+    double* staging = nullptr;  // pinned, 18 * npad doubles (per-sphere scalars at upload)
+    double* d_stage = nullptr;  // device, 6 x 3 npad doubles: AoS copies of the vec3 arrays
     double* h_energy = nullptr; // pinned, 8 doubles
     unsigned int* h_status = nullptr;
     bool uploaded = false;
@@ -138,33 +139,22 @@ int fetch_energy_and_status(sl_handle* h, sl_energy* out, bool want_energy)
     return SL_OK;
 }
 
-// AoS vec3[n] -> staging SoA rows (3 x npad) -> device Vec3Soa.
-int put_vec3(sl_handle* h, const double* aos, const sl::Vec3Soa& dst, double* stage)
+// True if no element is Inf or NaN (exponent field all ones); a branch-free
+// loop over the bit patterns, which the compiler vectorises.
+bool all_finite(const double* a, size_t count)
 {
-    const int n = h->sys.n, np = h->sys.npad;
-    for (int c = 0; c < 3; ++c) {
-        double* row = stage + (size_t)c * np;
-        for (int i = 0; i < n; ++i) row[i] = aos ? aos[3 * (size_t)i + c] : 0.0;
-        for (int i = n; i < np; ++i) row[i] = 0.0;
-        SL_CUDA(cudaMemcpyAsync(dst.c[c], row, np * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-    }
-    return SL_OK;
+    const uint64_t* u = reinterpret_cast<const uint64_t*>(a);
+    uint64_t bad = 0;
+    for (size_t i = 0; i < count; ++i) bad |= ((u[i] & 0x7ff0000000000000ull) == 0x7ff0000000000000ull) ? 1u : 0u;
+    return bad == 0;
 }
 
-int get_vec3(sl_handle* h, const sl::Vec3Soa& src, double* stage)
+// The six vec3 arrays a handle exchanges with its caller, in staging order.
+void stage_arrays(sl_handle* h, sl::Vec3Soa* out[6])
 {
-    const int np = h->sys.npad;
-    for (int c = 0; c < 3; ++c)
-        SL_CUDA(cudaMemcpyAsync(stage + (size_t)c * np, src.c[c], np * sizeof(double), cudaMemcpyDeviceToHost,
-                                h->stream));
-    return SL_OK;
-}
-
-void unstage_vec3(const sl_handle* h, const double* stage, double* aos)
-{
-    const int n = h->sys.n, np = h->sys.npad;
-    for (int c = 0; c < 3; ++c)
-        for (int i = 0; i < n; ++i) aos[3 * (size_t)i + c] = stage[(size_t)c * np + i];
+    sl::System& s = h->sys;
+    sl::Vec3Soa* a[6] = {&s.pos, &s.vel, &s.w, &s.acc, &s.aacc, &s.prev};
+    for (int k = 0; k < 6; ++k) out[k] = a[k];
 }
 
 void drop_graph(sl_handle* h)
@@ -236,6 +226,7 @@ int sl_create(int n, const sl_material* mat, int mode, sl_handle** out)
     const size_t o_en = take(8 * sizeof(double));
     const size_t o_st = take(sizeof(unsigned int));
     const size_t o_scl = take(sizeof(sl::Scalars));
+    const size_t o_dstage = take(6 * 3 * np * sizeof(double));
     h->arena_bytes = off;
     e = cudaMalloc(&h->arena, h->arena_bytes);
     if (e != cudaSuccess) { sl_destroy(h); return fail(SL_ERR_ALLOC, std::string("cudaMalloc: ") + cudaGetErrorString(e)); }
@@ -260,6 +251,7 @@ int sl_create(int n, const sl_material* mat, int mode, sl_handle** out)
     s.energy = reinterpret_cast<double*>(base + o_en);
     s.status = reinterpret_cast<unsigned int*>(base + o_st);
     h->d_sc = reinterpret_cast<sl::Scalars*>(base + o_scl);
+    h->d_stage = reinterpret_cast<double*>(base + o_dstage);
     s.sc = h->d_sc;
     if (mode == SL_MODE_EXACT) h->has_map = sl::make_pair_map(s, &h->pair_map);
     e = cudaMemsetAsync(h->arena, 0, h->arena_bytes, h->stream);
@@ -345,17 +337,23 @@ int sl_upload_resume(sl_handle* h, const double* pos, const double* vel, const d
     if (int r = check_handle(h)) return r;
     if (!pos || !vel || !w) return fail(SL_ERR_ARG, "pos, vel or w is NULL");
     const int n = h->sys.n;
-    for (int i = 0; i < 3 * n; ++i)
-        if (!std::isfinite(pos[i]) || !std::isfinite(vel[i]) || !std::isfinite(w[i]))
-            return fail(SL_ERR_ARG, "non-finite position, velocity or spin in input");
+    if (!all_finite(pos, 3 * (size_t)n) || !all_finite(vel, 3 * (size_t)n) || !all_finite(w, 3 * (size_t)n))
+        return fail(SL_ERR_ARG, "non-finite position, velocity or spin in input");
     const size_t np = h->sys.npad;
-    double* st = h->staging;
-    // each array has its own staging rows (copies are asynchronous)
-    const double* srcs[6] = {pos, vel, w, acc, aacc, pos_prev ? pos_prev : pos};
-    const sl::Vec3Soa* dsts[6] = {&h->sys.pos, &h->sys.vel, &h->sys.w, &h->sys.acc, &h->sys.aacc, &h->sys.prev};
-    for (int k = 0; k < 6; ++k) {
-        if (int r = put_vec3(h, srcs[k], *dsts[k], st + (size_t)(3 * k) * np)) return r;
-    }
+    // one copy per array into the device staging area; absent acc/aacc are
+    // zero, an absent previous position is the position
+    const double* srcs[6] = {pos, vel, w, acc, aacc, pos_prev};
+    unsigned present = 0;
+    for (int k = 0; k < 6; ++k)
+        if (srcs[k]) {
+            SL_CUDA(cudaMemcpyAsync(h->d_stage + (size_t)k * 3 * np, srcs[k], 3 * (size_t)n * sizeof(double),
+                                    cudaMemcpyHostToDevice, h->stream));
+            present |= 1u << k;
+        }
+    sl::Vec3Soa* dst[6];
+    stage_arrays(h, dst);
+    sl::launch_stage_in(h->sys, h->d_stage, dst, present, h->stream);
+    SL_CUDA(cudaGetLastError());
     SL_CUDA(cudaMemsetAsync(h->sys.status, 0, sizeof(unsigned int), h->stream));
     SL_CUDA(cudaStreamSynchronize(h->stream));
     h->forces_ready = (acc != nullptr && aacc != nullptr);
@@ -450,14 +448,20 @@ int sl_download(sl_handle* h, double* pos, double* vel, double* w, double* acc, 
 {
     if (int r = check_handle(h)) return r;
     double* outs[5] = {pos, vel, w, acc, aacc};
-    const sl::Vec3Soa* srcs[5] = {&h->sys.pos, &h->sys.vel, &h->sys.w, &h->sys.acc, &h->sys.aacc};
     const size_t np = h->sys.npad;
+    const int n = h->sys.n;
+    unsigned want = 0;
+    for (int k = 0; k < 5; ++k)
+        if (outs[k]) want |= 1u << k;
+    sl::Vec3Soa* src[6];
+    stage_arrays(h, src);
+    sl::launch_stage_out(h->sys, h->d_stage, src, want, h->stream);
+    SL_CUDA(cudaGetLastError());
     for (int k = 0; k < 5; ++k)
         if (outs[k])
-            if (int r = get_vec3(h, *srcs[k], h->staging + 3 * k * np)) return r;
+            SL_CUDA(cudaMemcpyAsync(outs[k], h->d_stage + (size_t)k * 3 * np, 3 * (size_t)n * sizeof(double),
+                                    cudaMemcpyDeviceToHost, h->stream));
     SL_CUDA(cudaStreamSynchronize(h->stream));
-    for (int k = 0; k < 5; ++k)
-        if (outs[k]) unstage_vec3(h, h->staging + 3 * k * np, outs[k]);
     return SL_OK;
 }
 
