@@ -45,6 +45,7 @@ extern "C" {
 #define SL_ERR_ALLOC 4      /* device or host allocation failed */
 #define SL_ERR_STATE 5      /* call out of order (e.g. step before upload) */
 #define SL_ERR_UNSUPPORTED 6
+#define SL_ERR_TIMEOUT 7     /* a kernel's bounded wait for its own asynchronous copies ran out */
 
 /* arithmetic modes of the pair step */
 #define SL_MODE_EXACT 0     /* FP64, reference operation order, bit-exact */

@@ -20,6 +20,7 @@ SL_ERR_NONFINITE = 3
 SL_ERR_ALLOC = 4
 SL_ERR_STATE = 5
 SL_ERR_UNSUPPORTED = 6
+SL_ERR_TIMEOUT = 7
 
 SL_MODE_EXACT = 0
 SL_MODE_MIXED = 1

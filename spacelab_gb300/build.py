@@ -32,6 +32,7 @@ NVCC_COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ff
 # Per-file arithmetic contract: the exact step must not contract a*b+c.
 NVCC_FILE_FLAGS = {
     "sl_step.cu": ["--fmad=false"],
+    "sl_rowsum_tma.cu": ["--fmad=false"],
     "sl_capi.cu": ["--fmad=false"],
     "sl_static.cu": ["--fmad=false"],
     "sl_batch.cu": ["--fmad=false"],

@@ -65,7 +65,7 @@ __device__ double pair_pass_mixed(const Batch& b, int off, int n, const Material
                     const float d2s = d2f_bits(d2, 2 * sh);
                     const float inv_d = rsqrtf(d2s);
                     const float dist_s = d2s * inv_d;
-                    const float ovl_s = d2f_bits(gap2, 2 * sh) / (Ras + Rbs + dist_s);
+                    const float ovl_s = __fdividef(d2f_bits(gap2, 2 * sh), Ras + Rbs + dist_s);
                     const float nx = rxs * inv_d, ny = rys * inv_d, nz = rzs * inv_d;
                     float fx, fy, fz;
                     if (gap2 > 0.0) {

@@ -61,7 +61,7 @@ struct sl_handle {
     cudaStream_t stream = nullptr;
     // exact mode: side stream + events overlapping row sums with pair phases
     sl::StepOverlap ov{};
-    CUtensorMap pair_map{};  // exact mode: the pair-term buffer for the TMA row sums
+    CUtensorMap pair_map{};  // the pair-term buffer for the TMA row sums
     bool has_map = false;
     bool has_ov = false;   // ov's stream and events exist
     bool overlap = false;  // steps use them
@@ -95,7 +95,7 @@ int check_handle(const sl_handle* h)
 void launch_mode_step(sl_handle* h, bool write, sl::StepTimers* tm)
 {
     if (h->mode == SL_MODE_MIXED)
-        sl::launch_step_mixed(h->sys, write, h->num_sms, h->stream, tm);
+        sl::launch_step_mixed(h->sys, write, h->num_sms, h->stream, tm, h->has_map ? &h->pair_map : nullptr);
     else
         sl::launch_step(h->sys, write, h->num_sms, h->stream, tm, h->overlap ? &h->ov : nullptr,
                         h->has_map ? &h->pair_map : nullptr);
@@ -134,7 +134,7 @@ int fetch_energy_and_status(sl_handle* h, sl_energy* out, bool want_energy)
         }
     }
     if (*h->h_status & sl::kStatusWaitTimeoutBit)
-        return fail(SL_ERR_CUDA, "a row-sum kernel's bounded wait for its TMA copies ran out");
+        return fail(SL_ERR_TIMEOUT, "a row-sum kernel's bounded wait for its TMA copies ran out");
     if (*h->h_status) return fail(SL_ERR_NONFINITE, "state became non-finite (NaN/Inf position, velocity or spin)");
     return SL_OK;
 }
@@ -253,7 +253,7 @@ int sl_create(int n, const sl_material* mat, int mode, sl_handle** out)
     h->d_sc = reinterpret_cast<sl::Scalars*>(base + o_scl);
     h->d_stage = reinterpret_cast<double*>(base + o_dstage);
     s.sc = h->d_sc;
-    if (mode == SL_MODE_EXACT) h->has_map = sl::make_pair_map(s, &h->pair_map);
+    h->has_map = sl::make_pair_map(s, mode == SL_MODE_MIXED, &h->pair_map);
     e = cudaMemsetAsync(h->arena, 0, h->arena_bytes, h->stream);
     if (e != cudaSuccess) { sl_destroy(h); return cuda_fail(e, "cudaMemset"); }
     e = cudaMallocHost(&h->staging, 18 * np * sizeof(double));

@@ -89,9 +89,9 @@ __device__ __forceinline__ double f2d_bits(float f)
     const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
     const unsigned e = (u >> 23) & 0xffu;
     const unsigned long long m = u & 0x7fffffu;
-    if (e == 0) return __longlong_as_double((long long)sign);
     const unsigned long long ed = (e == 0xffu) ? 0x7ffull : (unsigned long long)(e + 896u);
-    return __longlong_as_double((long long)(sign | (ed << 52) | (m << 29)));
+    const unsigned long long body = (e == 0u) ? 0ull : ((ed << 52) | (m << 29));  // select, no branch
+    return __longlong_as_double((long long)(sign | body));
 }
 
 // RN-even double -> float of x * 2^-shift (bit manipulation on the integer

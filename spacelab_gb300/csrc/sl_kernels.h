@@ -37,12 +37,20 @@ void launch_stage_out(const System& s, double* stage, Vec3Soa* const arr[6], uns
 // TMA-streamed row sums; NULL the plain-load form.
 void launch_step(const System& s, bool write, int num_sms, cudaStream_t st, StepTimers* tm,
                  const StepOverlap* ov = nullptr, const CUtensorMap* map = nullptr);
-// Encodes the pair-term buffer's tensor map; false if the driver offers no
-// tensor-map encoder (the plain-load row sums are used then).
-bool make_pair_map(const System& s, CUtensorMap* map);
+// Encodes the pair-term buffer's tensor map, FP64 terms (exact form) or FP32
+// terms (mixed form); false if the driver offers no tensor-map encoder (the
+// plain-load row sums are used then).
+bool make_pair_map(const System& s, bool fp32_terms, CUtensorMap* map);
+// The TMA-streamed ordered row sums over partner blocks [b0, b1) with terms
+// of type T (double: exact form, float: mixed form); first/last as for the
+// plain row sums.
+template <typename T>
+void launch_rowsum_tma(const System& s, const CUtensorMap& map, int b0, int b1, int first, int last, int num_sms,
+                       cudaStream_t st);
 // Status bit set by a kernel whose bounded wait for a TMA copy ran out.
 constexpr unsigned kStatusWaitTimeoutBit = 2u;
-void launch_step_mixed(const System& s, bool write, int num_sms, cudaStream_t st, StepTimers* tm);
+void launch_step_mixed(const System& s, bool write, int num_sms, cudaStream_t st, StepTimers* tm,
+                       const CUtensorMap* map = nullptr);
 void launch_drift(const System& s, cudaStream_t st);
 void launch_energy(const System& s, cudaStream_t st);
 int pair_grid_blocks(long long tiles, int num_sms);

@@ -1,0 +1,282 @@
+// sl_rowsum_tma.cu -- the ordered row sums (pass 2's accumulation, then
+// pass 3) with the pair-term rows streamed into shared memory by TMA, for
+// FP64 terms (exact form) and FP32 terms summed in FP64 (mixed form).
+//
+// Thread (c, i) adds acc_c[i] = sum over partners j ascending of
+// pairbuf[c][i][j] -- the order in which the reference adds terms to acc[i]
+// and aacc[i] (ColliderSingleCore.cpp:100-103, 249-250) -- over the partner
+// blocks [b0, b1), continuing the running sums kept in acc/aacc between
+// segments; the last segment does pass 3 (:263-267).
+//
+// Layout: one warp per (component, 32-row block), lane = row, kRsWarps
+// independent warps per CTA so that the warps and their FP64 add chains
+// spread over the SM's sub-partitions.  A stage of a warp's pipeline is one
+// TMA box: the warp's 32 rows x 128 bytes (16 doubles or 32 floats), stored
+// with the 128-byte swizzle so that the lanes' 16-byte reads of their own
+// rows fall in distinct bank groups (4 wavefronts per 512 bytes, the
+// minimum).  kRsStages boxes are in flight per warp; one lane issues the
+// copies and every wait is bounded (sl_tma.cuh): a copy that does not land
+// sets status bit 2 and the warp returns after draining its other copies.
+// A stage is one box or two (RsStage): with one, the footprint (12 KB of
+// shared memory and at most 128 registers per thread) lets 16 warps share
+// an SM, so that the 3n/32 warps of a system of up to ~26,000 spheres run in
+// one wave; with two, each stage wait covers twice the adds, which pays when
+// the warps are few.
+//
+// Every entry of a row is added, the row's own column and the padding
+// columns included: those are never written and hold +0.0 (a handle's arena
+// is zeroed at creation and n is fixed per handle), and adding +0.0 leaves
+// a sum that starts at +0.0 unchanged -- RN additions from +0.0 never give
+// -0.0.  The chain is then additions only, which the FP64 unit bounds.
+#include "sl_device.cuh"
+#include "sl_kernels.h"
+#include "sl_tma.cuh"
+
+#include <cudaTypedefs.h>
+#include <mutex>
+
+namespace sl {
+
+namespace {
+
+constexpr int kRsStages = 3;
+constexpr int kRsWarps = 2;
+constexpr int kRsBox = kBlock * 128;  // one 128-byte-wide box of 32 rows
+
+// BPS boxes per stage: 2 when a system's warps are few (each stage wait then
+// covers twice the adds), 1 when they are many (half the footprint, so that
+// up to 16 warps share an SM and large systems run in one wave).
+template <int BPS>
+struct RsStage {
+    static constexpr int kBytes = BPS * kRsBox;
+    static constexpr int kWarpBytes = kRsStages * kBytes;
+    static constexpr int kSmem = kRsWarps * kWarpBytes + 1024;  // + alignment slack
+    static constexpr int kChunks = BPS * 8;                     // 16-byte reads per lane per stage
+};
+
+// A lane's 16-byte chunk of its row -> its terms as doubles (2 doubles, or
+// 4 floats widened on the integer pipe).
+template <typename T>
+struct RsTerm;
+
+template <>
+struct RsTerm<double> {
+    static constexpr int kBoxCols = 16;  // columns per box (stage)
+    static constexpr int kPerChunk = 2;
+    static constexpr CUtensorMapDataType kType = CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+    __device__ static void unpack(const uint4& u, double* v)
+    {
+        v[0] = __hiloint2double((int)u.y, (int)u.x);
+        v[1] = __hiloint2double((int)u.w, (int)u.z);
+    }
+    __device__ static double widen(double x) { return x; }
+};
+
+template <>
+struct RsTerm<float> {
+    static constexpr int kBoxCols = 32;
+    static constexpr int kPerChunk = 4;
+    static constexpr CUtensorMapDataType kType = CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    __device__ static void unpack(const uint4& u, double* v)
+    {
+        v[0] = f2d_bits(__uint_as_float(u.x));
+        v[1] = f2d_bits(__uint_as_float(u.y));
+        v[2] = f2d_bits(__uint_as_float(u.z));
+        v[3] = f2d_bits(__uint_as_float(u.w));
+    }
+    __device__ static double widen(float x) { return f2d_bits(x); }
+};
+
+template <typename T, int BPS>
+__device__ __forceinline__ void rs_issue(unsigned char* buf, uint64_t* full, const CUtensorMap* map, int q, int x0,
+                                         int row0)
+{
+    const int st = q % kRsStages;
+    unsigned char* dst = buf + st * RsStage<BPS>::kBytes;
+    tma::mbar_arrive_expect_tx(&full[st], RsStage<BPS>::kBytes);
+#pragma unroll
+    for (int b = 0; b < BPS; ++b)
+        tma::load_2d(dst + b * kRsBox, map, x0 + (q * BPS + b) * RsTerm<T>::kBoxCols, row0, &full[st]);
+}
+
+// lane's 16-byte chunk k of its own row in a stage buffer (swizzled boxes)
+__device__ __forceinline__ uint4 rs_chunk(const unsigned char* stage, int lane, int k)
+{
+    return *reinterpret_cast<const uint4*>(stage + (k >> 3) * kRsBox + lane * 128 + (((k & 7) ^ (lane & 7)) << 4));
+}
+
+template <typename T, int BPS>
+__global__ void __launch_bounds__(32 * kRsWarps, 8 / BPS) rowsum_tma_kernel(const __grid_constant__ System s,
+                                                                            const __grid_constant__ CUtensorMap map,
+                                                                            int b0, int b1, int first, int last)
+{
+    using Stage = RsStage<BPS>;
+    constexpr int kStageCols = BPS * RsTerm<T>::kBoxCols;
+    // stages per 32-column partner block (1 when a stage spans several blocks)
+    constexpr int kSpb = kStageCols >= kBlock ? 1 : kBlock / kStageCols;
+    constexpr int kBps = kStageCols >= kBlock ? kStageCols / kBlock : 1;  // partner blocks per stage
+    constexpr int kPer = RsTerm<T>::kPerChunk;
+    extern __shared__ unsigned char rs_raw[];
+    __shared__ __align__(8) uint64_t full_all[kRsWarps][kRsStages];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int wg = blockIdx.x * kRsWarps + warp;  // global (component, row block) index
+    if (wg >= 3 * s.nb) return;                   // no block-wide synchronisation below
+    unsigned char* buf = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(rs_raw) + 1023) &
+                                                          ~static_cast<uintptr_t>(1023)) +
+                         warp * Stage::kWarpBytes;
+    uint64_t* full = full_all[warp];
+    const int c = wg / s.nb;
+    const int rb = wg - c * s.nb;
+    const int i = rb * kBlock + lane;  // < npad
+    const int row0 = c * s.npad + rb * kBlock;
+    const int x0 = b0 * kBlock;
+    const int nq = (b1 - b0) * kSpb / kBps;  // callers give whole stages
+    if (lane == 0) {
+        for (int k = 0; k < kRsStages; ++k) tma::mbar_init(&full[k], 1);
+        tma::fence_barrier_init();
+        for (int q = 0; q < nq && q < kRsStages; ++q) rs_issue<T, BPS>(buf, full, &map, q, x0, row0);
+    }
+    __syncwarp();
+
+    double acc = first ? 0.0 : s.acc.c[c][i];
+    double aacc = first ? 0.0 : s.aacc.c[c][i];
+    // torque terms: contact partners only, in the same ascending order, after
+    // each partner block's force terms; the contact-mask word of the next
+    // partner block is loaded a block ahead
+    const size_t plane = (size_t)s.npad * s.npad;
+    const uint32_t* mrow = s.cmask + (size_t)i * s.nb;  // rows < npad exist; padding rows are 0
+    const T* trow = reinterpret_cast<const T*>(s.torqbuf) + c * plane + (size_t)i * s.npad;
+    uint32_t wnext = b1 > b0 ? mrow[b0] : 0u;
+    // Software pipeline: stage q is in registers (cur) while its buffer is
+    // refilled and stage q+1 is read into nxt, so the add chain never waits
+    // for a barrier or for shared memory.
+    uint4 cur[Stage::kChunks], nxt[Stage::kChunks];
+    int waited = 0;  // first stage not yet observed complete
+    bool ok = nq <= 0 || __all_sync(0xffffffffu, tma::mbar_wait(&full[0], 0));
+    if (ok && nq > 0) {
+#pragma unroll
+        for (int k = 0; k < Stage::kChunks; ++k) cur[k] = rs_chunk(buf, lane, k);
+        waited = 1;
+    }
+    for (int q = 0; ok && q < nq; ++q) {
+        __syncwarp();  // every lane has stage q in registers: its buffer is free
+        if (lane == 0 && q + kRsStages < nq) {
+            tma::fence_proxy_async();
+            rs_issue<T, BPS>(buf, full, &map, q + kRsStages, x0, row0);
+        }
+        if (q + 1 < nq) {
+            const int st1 = (q + 1) % kRsStages;
+            ok = __all_sync(0xffffffffu, tma::mbar_wait(&full[st1], ((q + 1) / kRsStages) & 1));
+            if (ok) {
+#pragma unroll
+                for (int k = 0; k < Stage::kChunks; ++k) nxt[k] = rs_chunk(buf + st1 * Stage::kBytes, lane, k);
+                waited = q + 2;
+            }
+        }
+#pragma unroll
+        for (int pb = 0; pb < kBps; ++pb) {  // each partner block in the stage
+            constexpr int kChunksPerBlock = Stage::kChunks / kBps;
+#pragma unroll
+            for (int k = pb * kChunksPerBlock; k < (pb + 1) * kChunksPerBlock; ++k) {
+                double v[kPer];
+                RsTerm<T>::unpack(cur[k], v);
+#pragma unroll
+                for (int e = 0; e < kPer; ++e) acc += v[e];
+            }
+            if (q % kSpb == kSpb - 1) {  // partner block Y complete: its torque terms
+                const int Y = b0 + (q / kSpb) * kBps + pb;
+                uint32_t wd = wnext;
+                if (Y + 1 < b1) wnext = mrow[Y + 1];
+                while (wd) {
+                    const int bit = __ffs(wd) - 1;
+                    wd &= wd - 1;
+                    aacc += RsTerm<T>::widen(trow[Y * kBlock + bit]);
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < Stage::kChunks; ++k) cur[k] = nxt[k];
+    }
+    if (!ok) {
+        // a wait ran out: drain the copies still in flight (each wait
+        // bounded), then report.  Stages waited .. waited + kRsStages - 1 may
+        // have been issued (every stage before `waited` was observed).
+        const int issued = min(nq, waited + kRsStages);
+        for (int qq = waited; qq < issued; ++qq) tma::mbar_wait(&full[qq % kRsStages], (qq / kRsStages) & 1);
+        if (lane == 0) atomicOr(s.status, kStatusWaitTimeoutBit);
+        return;
+    }
+    if (i >= s.n) return;
+    s.acc.c[c][i] = acc;
+    s.aacc.c[c][i] = aacc;
+    if (!last) return;
+    const double dt = s.sc->dt;
+    const double v = s.velh.c[c][i] + (.5 * acc) * dt;    // :265
+    const double wv = s.wh.c[c][i] + (.5 * aacc) * dt;    // :266
+    s.vel.c[c][i] = v;
+    s.w.c[c][i] = wv;
+    if (!isfinite(v) || !isfinite(wv) || !isfinite(s.pos.c[c][i])) atomicOr(s.status, 1u);
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    });
+    return encode;
+}
+
+// The pair-term buffer [3][npad][npad] as a 2D tensor of 3 npad rows of npad
+// columns; boxes of 128 bytes x 32 rows with the 128-byte swizzle.
+template <typename T>
+bool make_map(const System& s, CUtensorMap* map)
+{
+    PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
+    if (!encode || !s.pairbuf) return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)s.npad, (cuuint64_t)3 * s.npad};
+    const cuuint64_t strides[1] = {(cuuint64_t)s.npad * sizeof(T)};
+    const cuuint32_t box[2] = {(cuuint32_t)RsTerm<T>::kBoxCols, (cuuint32_t)kBlock};
+    const cuuint32_t estr[2] = {1, 1};
+    if (encode(map, RsTerm<T>::kType, 2, s.pairbuf, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) !=
+        CUDA_SUCCESS)
+        return false;
+    return cudaFuncSetAttribute(rowsum_tma_kernel<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                RsStage<1>::kSmem) == cudaSuccess &&
+           cudaFuncSetAttribute(rowsum_tma_kernel<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                RsStage<2>::kSmem) == cudaSuccess;
+}
+
+}  // namespace
+
+bool make_pair_map(const System& s, bool fp32_terms, CUtensorMap* map)
+{
+    return fp32_terms ? make_map<float>(s, map) : make_map<double>(s, map);
+}
+
+template <typename T>
+void launch_rowsum_tma(const System& s, const CUtensorMap& map, int b0, int b1, int first, int last, int num_sms,
+                       cudaStream_t st)
+{
+    const int ctas = (3 * s.nb + kRsWarps - 1) / kRsWarps;
+    // two-box stages while every warp fits at 4 CTAs (8 warps) per SM and the
+    // partner range is whole stages; one-box stages otherwise
+    const bool wide = ctas <= 4 * num_sms && (RsTerm<T>::kBoxCols * 2 <= kBlock || (b1 - b0) % 2 == 0);
+    if (wide)
+        rowsum_tma_kernel<T, 2><<<ctas, 32 * kRsWarps, RsStage<2>::kSmem, st>>>(s, map, b0, b1, first, last);
+    else
+        rowsum_tma_kernel<T, 1><<<ctas, 32 * kRsWarps, RsStage<1>::kSmem, st>>>(s, map, b0, b1, first, last);
+}
+
+template void launch_rowsum_tma<double>(const System&, const CUtensorMap&, int, int, int, int, int, cudaStream_t);
+template void launch_rowsum_tma<float>(const System&, const CUtensorMap&, int, int, int, int, int, cudaStream_t);
+
+}  // namespace sl

@@ -2,7 +2,7 @@
 // with the reference's sim_one_step (ColliderSingleCore.cpp:78-288).
 //
 // One step is four launches on the handle's stream (the row sums have a
-// TMA-streamed form, rowsum_tma_kernel, used whenever a tensor map of the
+// TMA-streamed form in sl_rowsum_tma.cu, used whenever a tensor map of the
 // pair-term buffer could be made):
 //   drift_kernel      pass 1 (ColliderSingleCore.cpp:82-97): velh, wh, drift,
 //                     and the previous positions that replace the reference's
@@ -29,11 +29,8 @@
 #include "sl_kernels.h"
 #include "sl_fp64_exact.cuh"
 #include "sl_pair_exact.cuh"
-#include "sl_tma.cuh"
 
 #include <cstdio>
-#include <cudaTypedefs.h>
-#include <mutex>
 
 namespace sl {
 
@@ -290,140 +287,6 @@ __global__ void __launch_bounds__(kRowThreads) rowsum_kernel(const __grid_consta
     if (!isfinite(v) || !isfinite(wv) || !isfinite(s.pos.c[c][i])) atomicOr(s.status, 1u);
 }
 
-// ------------------------------------------- row sums, TMA-streamed form --
-// The same sums in the same order as rowsum_kernel, for a handle's own
-// arena (whose never-written pair-term entries are +0.0), with the
-// pair-term rows streamed into shared memory by TMA: one warp per
-// (component, 32-row block), lane = row, kRsWarps independent warps per CTA
-// so that the warps (and their FP64 add chains) spread over the SM's four
-// sub-partitions.  Stage q of the pipeline holds partner block b0 + q
-// as two 16-column boxes of the warp's 32 rows (8 KB), stored with the
-// 128-byte swizzle so that the lanes' 16-byte reads of their own rows fall
-// in distinct bank groups (4 wavefronts per 512 bytes, the minimum).
-// kRsStages stages are in flight; one lane issues the copies.  A copy that
-// does not land within the bounded wait sets status bit 2 and the warp
-// returns after draining its other copies.
-constexpr int kRsStages = 3;
-constexpr int kRsWarps = 2;  // independent warps per CTA (each on its own SM sub-partition)
-constexpr int kRsBox = kBlock * 128;  // one 16-column box of 32 rows
-constexpr int kRsStageBytes = 2 * kRsBox;
-constexpr int kRsWarpBytes = kRsStages * kRsStageBytes;
-constexpr int kRsSmem = kRsWarps * kRsWarpBytes + 1024;  // + alignment slack
-
-__device__ __forceinline__ void rs_issue(unsigned char* buf, uint64_t* full, const CUtensorMap* map, int q,
-                                         int Y, int row0)
-{
-    const int st = q % kRsStages;
-    unsigned char* dst = buf + st * kRsStageBytes;
-    tma::mbar_arrive_expect_tx(&full[st], kRsStageBytes);
-    tma::load_2d(dst, map, Y * kBlock, row0, &full[st]);
-    tma::load_2d(dst + kRsBox, map, Y * kBlock + 16, row0, &full[st]);
-}
-
-__global__ void __launch_bounds__(32 * kRsWarps) rowsum_tma_kernel(const __grid_constant__ System s,
-                                                                   const __grid_constant__ CUtensorMap map, int b0,
-                                                                   int b1, int first, int last)
-{
-    extern __shared__ unsigned char rs_raw[];
-    __shared__ __align__(8) uint64_t full_all[kRsWarps][kRsStages];
-    const int lane = threadIdx.x & 31;
-    const int warp = threadIdx.x >> 5;
-    const int wg = blockIdx.x * kRsWarps + warp;  // global (component, row block) index
-    if (wg >= 3 * s.nb) return;                   // no block-wide synchronisation below
-    unsigned char* buf = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(rs_raw) + 1023) &
-                                                          ~static_cast<uintptr_t>(1023)) +
-                         warp * kRsWarpBytes;
-    uint64_t* full = full_all[warp];
-    const int c = wg / s.nb;
-    const int rb = wg - c * s.nb;
-    const int i = rb * kBlock + lane;  // < npad
-    const int row0 = c * s.npad + rb * kBlock;
-    const int nq = b1 - b0;
-    const int n = s.n;
-    if (lane == 0) {
-        for (int k = 0; k < kRsStages; ++k) tma::mbar_init(&full[k], 1);
-        tma::fence_barrier_init();
-        for (int q = 0; q < nq && q < kRsStages; ++q) rs_issue(buf, full, &map, q, b0 + q, row0);
-    }
-    __syncwarp();
-
-    // Software pipeline: stage q's 32 values are in registers (cur) while
-    // its buffer is already refilled and stage q+1 is read; the dependent
-    // add chain thus never waits for shared memory.
-    double acc = first ? 0.0 : s.acc.c[c][i];
-    double aacc = first ? 0.0 : s.aacc.c[c][i];
-    // torque terms: contact partners only, in the same ascending order; the
-    // contact-mask word of the next partner block is loaded a stage ahead
-    const size_t plane = (size_t)s.npad * s.npad;
-    const uint32_t* mrow = s.cmask + (size_t)i * s.nb;  // rows < npad exist; padding rows are 0
-    const double* trow = s.torqbuf + c * plane + (size_t)i * s.npad;
-    uint32_t wnext = nq > 0 ? mrow[b0] : 0u;
-    double2 cur[16], nxt[16];
-    bool ok = nq <= 0 || __all_sync(0xffffffffu, tma::mbar_wait(&full[0], 0));
-    if (ok && nq > 0) {
-#pragma unroll
-        for (int k = 0; k < 16; ++k)
-            cur[k] = *reinterpret_cast<const double2*>(buf + lane * 128 + (k >> 3) * kRsBox + (((k & 7) ^ (lane & 7)) << 4));
-    }
-    int q = 0;
-    for (; ok && q < nq; ++q) {
-        __syncwarp();  // every lane has stage q in registers: its buffer is free
-        if (lane == 0 && q + kRsStages < nq) {
-            tma::fence_proxy_async();
-            rs_issue(buf, full, &map, q + kRsStages, b0 + q + kRsStages, row0);
-        }
-        if (q + 1 < nq) {
-            const int st1 = (q + 1) % kRsStages;
-            ok = __all_sync(0xffffffffu, tma::mbar_wait(&full[st1], ((q + 1) / kRsStages) & 1));
-            if (ok) {
-                const unsigned char* row = buf + st1 * kRsStageBytes + lane * 128;
-#pragma unroll
-                for (int k = 0; k < 16; ++k)
-                    nxt[k] = *reinterpret_cast<const double2*>(row + (k >> 3) * kRsBox + (((k & 7) ^ (lane & 7)) << 4));
-            }
-        }
-        // Every entry is added, the row's own column and the padding columns
-        // included: those are never written and hold +0.0 (the arena is
-        // zeroed at creation and n is fixed per handle), and adding +0.0
-        // leaves the sum unchanged -- a sum of RN additions that starts at
-        // +0.0 is never -0.0.  The chain is then DADDs only.
-        const int jb = (b0 + q) * kBlock;
-        uint32_t wd = wnext;
-        if (q + 1 < nq) wnext = mrow[b0 + q + 1];
-#pragma unroll
-        for (int k = 0; k < 16; ++k) {
-            acc += cur[k].x;
-            acc += cur[k].y;
-        }
-        while (wd) {
-            const int bit = __ffs(wd) - 1;
-            wd &= wd - 1;
-            aacc += trow[jb + bit];
-        }
-#pragma unroll
-        for (int k = 0; k < 16; ++k) cur[k] = nxt[k];
-    }
-    // on a failed wait q is the first stage not observed complete
-    if (!ok) {
-        // drain the copies still in flight (each wait bounded), then report;
-        // stages q .. q + kRsStages - 1 may have been issued
-        const int issued = min(nq, q + kRsStages);
-        for (int qq = q; qq < issued; ++qq) tma::mbar_wait(&full[qq % kRsStages], (qq / kRsStages) & 1);
-        if (lane == 0) atomicOr(s.status, kStatusWaitTimeoutBit);
-        return;
-    }
-    if (i >= n) return;
-    s.acc.c[c][i] = acc;
-    s.aacc.c[c][i] = aacc;
-    if (!last) return;
-    const double dt = s.sc->dt;
-    const double v = s.velh.c[c][i] + (.5 * acc) * dt;    // :265
-    const double wv = s.wh.c[c][i] + (.5 * aacc) * dt;    // :266
-    s.vel.c[c][i] = v;
-    s.w.c[c][i] = wv;
-    if (!isfinite(v) || !isfinite(wv) || !isfinite(s.pos.c[c][i])) atomicOr(s.status, 1u);
-}
-
 // ------------------------------------------------------ energy totals -----
 constexpr int kRedThreads = 256;
 
@@ -591,39 +454,11 @@ void launch_energy(const System& s, cudaStream_t st)
     energy_final_kernel<<<1, kRedThreads, 0, st>>>(s, nred);
 }
 
-// The pair-term buffer [3][npad][npad] as a 2D FP64 tensor of 3*npad rows
-// of npad columns, boxes of 16 columns x 32 rows with the 128-byte swizzle.
-bool make_pair_map(const System& s, CUtensorMap* map)
-{
-    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
-    static std::once_flag once;
-    std::call_once(once, [] {
-        void* fn = nullptr;
-        cudaDriverEntryPointQueryResult q{};
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
-    });
-    if (!encode || !s.pairbuf) return false;
-    const cuuint64_t dims[2] = {(cuuint64_t)s.npad, (cuuint64_t)3 * s.npad};
-    const cuuint64_t strides[1] = {(cuuint64_t)s.npad * sizeof(double)};
-    const cuuint32_t box[2] = {16, (cuuint32_t)kBlock};
-    const cuuint32_t estr[2] = {1, 1};
-    if (encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, s.pairbuf, dims, strides, box, estr,
-               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-        return false;
-    return cudaFuncSetAttribute(rowsum_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kRsSmem) ==
-           cudaSuccess;
-}
-
 static void launch_rowsum(const System& s, cudaStream_t st, const CUtensorMap* map, int b0, int b1, int first,
-                          int last)
+                          int last, int num_sms)
 {
     if (map)
-        rowsum_tma_kernel<<<(3 * s.nb + kRsWarps - 1) / kRsWarps, 32 * kRsWarps, kRsSmem, st>>>(s, *map, b0, b1,
-                                                                                            first, last);
+        launch_rowsum_tma<double>(s, *map, b0, b1, first, last, num_sms, st);
     else
         rowsum_kernel<<<(3 * s.n + kRowThreads - 1) / kRowThreads, kRowThreads, 0, st>>>(s, b0, b1, first, last);
 }
@@ -649,13 +484,13 @@ void launch_step(const System& s, bool write, int num_sms, cudaStream_t st, Step
     if (np <= 1) {
         launch_pair_columns(s, write, num_sms, st, 0, s.nb);
         if (tm) cudaEventRecord(tm->ev[1], st);
-        launch_rowsum(s, st, map, 0, s.nb, 1, 1);
+        launch_rowsum(s, st, map, 0, s.nb, 1, 1, num_sms);
     } else {
         for (int p = 0; p < np; ++p) {
             launch_pair_columns(s, write, num_sms, st, cb[p], cb[p + 1]);
             cudaEventRecord(ov->phase[p], st);
             cudaStreamWaitEvent(ov->side, ov->phase[p], 0);
-            launch_rowsum(s, ov->side, map, cb[p], cb[p + 1], p == 0, p == np - 1);
+            launch_rowsum(s, ov->side, map, cb[p], cb[p + 1], p == 0, p == np - 1, num_sms);
         }
         if (tm) cudaEventRecord(tm->ev[1], st);
         cudaEventRecord(ov->join, ov->side);

@@ -35,7 +35,7 @@ struct ABlockMixed {
 // tile, lane b = sphere 32Y+b, loop over the A block; terms stored as FP32
 // in the [3][npad][npad] float view of pairbuf/torqbuf.
 template <bool WRITE>
-__global__ void __launch_bounds__(128, 3) mixed_pair_kernel(const __grid_constant__ System s)
+__global__ void __launch_bounds__(128, 4) mixed_pair_kernel(const __grid_constant__ System s)
 {
     __shared__ ABlockMixed sA[4];
     const int lane = threadIdx.x & 31;
@@ -84,10 +84,12 @@ __global__ void __launch_bounds__(128, 3) mixed_pair_kernel(const __grid_constan
                 const float inv_d = rsqrtf(d2s);
                 const float dist_s = d2s * inv_d;
                 const float Ras = ab.Rs[a];
-                const float ovl_s = d2f_bits(gap2, 2 * sh) / (Ras + Rbs + dist_s);
+                const float ovl_s = __fdividef(d2f_bits(gap2, 2 * sh), Ras + Rbs + dist_s);
                 const float nx = rxs * inv_d, ny = rys * inv_d, nz = rzs * inv_d;
                 float fx, fy, fz;
-                if (gap2 > 0.0) {
+                // gap2 > 0 on the bit pattern (integer pipe); NaN excluded
+                const long long gb = __double_as_longlong(gap2);
+                if (gb > 0 && gb <= 0x7ff0000000000000ll) {
                     contact = true;
                     const ContactIn in = gather_contact(s, A, B);
                     const ContactF o = contact_mixed(in, s.mat, sh, d2, nx, ny, nz, dist_s * L, ovl_s * L, Ras, Rbs);
@@ -189,19 +191,23 @@ __global__ void __launch_bounds__(kMixThreads) mixed_rowsum_kernel(const __grid_
 
 }  // namespace
 
-void launch_step_mixed(const System& s, bool write, int num_sms, cudaStream_t st, StepTimers* tm)
+void launch_step_mixed(const System& s, bool write, int num_sms, cudaStream_t st, StepTimers* tm,
+                       const CUtensorMap* map)
 {
     launch_drift(s, st);
     if (tm) cudaEventRecord(tm->ev[0], st);
     long long want = (s.ntiles + 3) / 4;
-    long long cap = (long long)num_sms * 3;
+    long long cap = (long long)num_sms * 4;  // 4 CTAs (16 warps) per SM
     const int pb = (int)(want < cap ? want : cap);
     if (write)
         mixed_pair_kernel<true><<<pb, 128, 0, st>>>(s);
     else
         mixed_pair_kernel<false><<<pb, 128, 0, st>>>(s);
     if (tm) cudaEventRecord(tm->ev[1], st);
-    mixed_rowsum_kernel<<<(3 * s.n + kMixThreads - 1) / kMixThreads, kMixThreads, 0, st>>>(s);
+    if (map)
+        launch_rowsum_tma<float>(s, *map, 0, s.nb, 1, 1, num_sms, st);
+    else
+        mixed_rowsum_kernel<<<(3 * s.n + kMixThreads - 1) / kMixThreads, kMixThreads, 0, st>>>(s);
     if (tm) cudaEventRecord(tm->ev[2], st);
     if (write) launch_energy(s, st);
 }
