@@ -215,9 +215,9 @@ int sl_create(int n, const sl_material* mat, int mode, sl_handle** out)
         for (int c = 0; c < 3; ++c) o_vec[v][c] = take(np * sizeof(double));
     size_t o_sc[8];
     for (int k = 0; k < 8; ++k) o_sc[k] = take(np * sizeof(double));
-    size_t o_f[3] = {0, 0, 0};
+    size_t o_f[10] = {};
     if (mode == SL_MODE_MIXED)
-        for (int k = 0; k < 3; ++k) o_f[k] = take(np * sizeof(float));
+        for (int k = 0; k < 10; ++k) o_f[k] = take(np * sizeof(float));
     const size_t o_pair = take(3 * np * np * sizeof(double));
     const size_t o_torq = take(3 * np * np * sizeof(double));
     const size_t o_mask = take(np * s.nb * sizeof(uint32_t));
@@ -242,6 +242,8 @@ int sl_create(int n, const sl_material* mat, int mode, sl_handle** out)
         s.f_R = reinterpret_cast<float*>(base + o_f[0]);
         s.f_inv_m = reinterpret_cast<float*>(base + o_f[1]);
         s.f_inv_moi = reinterpret_cast<float*>(base + o_f[2]);
+        s.f_Rlo = reinterpret_cast<float*>(base + o_f[3]);
+        for (int k = 0; k < 6; ++k) s.f_pos[k] = reinterpret_cast<float*>(base + o_f[4 + k]);
     }
     s.pairbuf = reinterpret_cast<double*>(base + o_pair);
     s.torqbuf = reinterpret_cast<double*>(base + o_torq);

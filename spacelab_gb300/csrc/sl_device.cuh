@@ -56,6 +56,10 @@ struct System {
     // mixed-precision form: per-sphere FP32 constants in lengths scaled by
     // 2^-len_shift (a power of two near the largest radius); NULL otherwise
     float *f_R, *f_inv_m, *f_inv_moi;
+    // and double-float (hi + lo) copies of the scaled radii's low parts and
+    // of the scaled positions (x, y, z hi, then x, y, z lo), the latter
+    // written by the drift kernel every step
+    float *f_Rlo, *f_pos[6];
     int len_shift;
 };
 

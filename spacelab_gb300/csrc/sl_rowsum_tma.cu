@@ -6,7 +6,9 @@
 // pairbuf[c][i][j] -- the order in which the reference adds terms to acc[i]
 // and aacc[i] (ColliderSingleCore.cpp:100-103, 249-250) -- over the partner
 // blocks [b0, b1), continuing the running sums kept in acc/aacc between
-// segments; the last segment does pass 3 (:263-267).
+// segments; the last segment does pass 3 (:263-267).  FP64 terms are added
+// in FP64 (the reference's own additions); the mixed form's FP32 terms are
+// added in a compensated double-float sum on the FP32 pipe.
 //
 // Layout: one warp per (component, 32-row block), lane = row, kRsWarps
 // independent warps per CTA so that the warps and their FP64 add chains
@@ -27,9 +29,11 @@
 // columns included: those are never written and hold +0.0 (a handle's arena
 // is zeroed at creation and n is fixed per handle), and adding +0.0 leaves
 // a sum that starts at +0.0 unchanged -- RN additions from +0.0 never give
-// -0.0.  The chain is then additions only, which the FP64 unit bounds.
+// -0.0.  The chain is then additions only, which for FP64 terms the FP64
+// unit bounds.
 #include "sl_device.cuh"
 #include "sl_kernels.h"
+#include "sl_df.cuh"
 #include "sl_tma.cuh"
 
 #include <cudaTypedefs.h>
@@ -54,37 +58,52 @@ struct RsStage {
     static constexpr int kChunks = BPS * 8;                     // 16-byte reads per lane per stage
 };
 
-// A lane's 16-byte chunk of its row -> its terms as doubles (2 doubles, or
-// 4 floats widened on the integer pipe).
+// Term type -> box width and the running-sum type a lane's 16-byte chunks
+// of its row are added into.
 template <typename T>
 struct RsTerm;
 
 template <>
 struct RsTerm<double> {
     static constexpr int kBoxCols = 16;  // columns per box (stage)
-    static constexpr int kPerChunk = 2;
     static constexpr CUtensorMapDataType kType = CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
-    __device__ static void unpack(const uint4& u, double* v)
-    {
-        v[0] = __hiloint2double((int)u.y, (int)u.x);
-        v[1] = __hiloint2double((int)u.w, (int)u.z);
-    }
-    __device__ static double widen(double x) { return x; }
+    // FP64 running sum: the reference's additions, in its order
+    struct Acc {
+        double a;
+        __device__ void start(double x) { a = x; }
+        __device__ void add_chunk(const uint4& u)
+        {
+            a += __hiloint2double((int)u.y, (int)u.x);
+            a += __hiloint2double((int)u.w, (int)u.z);
+        }
+        __device__ void add_term(double x) { a += x; }
+        __device__ double value() const { return a; }
+    };
 };
 
 template <>
 struct RsTerm<float> {
     static constexpr int kBoxCols = 32;
-    static constexpr int kPerChunk = 4;
     static constexpr CUtensorMapDataType kType = CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
-    __device__ static void unpack(const uint4& u, double* v)
-    {
-        v[0] = f2d_bits(__uint_as_float(u.x));
-        v[1] = f2d_bits(__uint_as_float(u.y));
-        v[2] = f2d_bits(__uint_as_float(u.z));
-        v[3] = f2d_bits(__uint_as_float(u.w));
-    }
-    __device__ static double widen(float x) { return f2d_bits(x); }
+    // compensated FP32 running sum (double-float, sl_df.cuh) on the FP32
+    // pipe, in ascending partner order; converted to FP64 at the end
+    struct Acc {
+        df::Sum a;
+        __device__ void start(double x)
+        {
+            const float h = d2f_bits(x, 0);
+            a = {h, d2f_bits(x - f2d_bits(h), 0)};
+        }
+        __device__ void add_chunk(const uint4& u)
+        {
+            a.add(__uint_as_float(u.x));
+            a.add(__uint_as_float(u.y));
+            a.add(__uint_as_float(u.z));
+            a.add(__uint_as_float(u.w));
+        }
+        __device__ void add_term(float x) { a.add(x); }
+        __device__ double value() const { return f2d_bits(a.s) + f2d_bits(a.c); }
+    };
 };
 
 template <typename T, int BPS>
@@ -115,7 +134,6 @@ __global__ void __launch_bounds__(32 * kRsWarps, 8 / BPS) rowsum_tma_kernel(cons
     // stages per 32-column partner block (1 when a stage spans several blocks)
     constexpr int kSpb = kStageCols >= kBlock ? 1 : kBlock / kStageCols;
     constexpr int kBps = kStageCols >= kBlock ? kStageCols / kBlock : 1;  // partner blocks per stage
-    constexpr int kPer = RsTerm<T>::kPerChunk;
     extern __shared__ unsigned char rs_raw[];
     __shared__ __align__(8) uint64_t full_all[kRsWarps][kRsStages];
     const int lane = threadIdx.x & 31;
@@ -139,8 +157,9 @@ __global__ void __launch_bounds__(32 * kRsWarps, 8 / BPS) rowsum_tma_kernel(cons
     }
     __syncwarp();
 
-    double acc = first ? 0.0 : s.acc.c[c][i];
-    double aacc = first ? 0.0 : s.aacc.c[c][i];
+    typename RsTerm<T>::Acc acc, aacc;
+    acc.start(first ? 0.0 : s.acc.c[c][i]);
+    aacc.start(first ? 0.0 : s.aacc.c[c][i]);
     // torque terms: contact partners only, in the same ascending order, after
     // each partner block's force terms; the contact-mask word of the next
     // partner block is loaded a block ahead
@@ -179,10 +198,7 @@ __global__ void __launch_bounds__(32 * kRsWarps, 8 / BPS) rowsum_tma_kernel(cons
             constexpr int kChunksPerBlock = Stage::kChunks / kBps;
 #pragma unroll
             for (int k = pb * kChunksPerBlock; k < (pb + 1) * kChunksPerBlock; ++k) {
-                double v[kPer];
-                RsTerm<T>::unpack(cur[k], v);
-#pragma unroll
-                for (int e = 0; e < kPer; ++e) acc += v[e];
+                acc.add_chunk(cur[k]);
             }
             if (q % kSpb == kSpb - 1) {  // partner block Y complete: its torque terms
                 const int Y = b0 + (q / kSpb) * kBps + pb;
@@ -191,7 +207,7 @@ __global__ void __launch_bounds__(32 * kRsWarps, 8 / BPS) rowsum_tma_kernel(cons
                 while (wd) {
                     const int bit = __ffs(wd) - 1;
                     wd &= wd - 1;
-                    aacc += RsTerm<T>::widen(trow[Y * kBlock + bit]);
+                    aacc.add_term(trow[Y * kBlock + bit]);
                 }
             }
         }
@@ -208,12 +224,13 @@ __global__ void __launch_bounds__(32 * kRsWarps, 8 / BPS) rowsum_tma_kernel(cons
         return;
     }
     if (i >= s.n) return;
-    s.acc.c[c][i] = acc;
-    s.aacc.c[c][i] = aacc;
+    const double fa = acc.value(), ta = aacc.value();
+    s.acc.c[c][i] = fa;
+    s.aacc.c[c][i] = ta;
     if (!last) return;
     const double dt = s.sc->dt;
-    const double v = s.velh.c[c][i] + (.5 * acc) * dt;    // :265
-    const double wv = s.wh.c[c][i] + (.5 * aacc) * dt;    // :266
+    const double v = s.velh.c[c][i] + (.5 * fa) * dt;    // :265
+    const double wv = s.wh.c[c][i] + (.5 * ta) * dt;     // :266
     s.vel.c[c][i] = v;
     s.w.c[c][i] = wv;
     if (!isfinite(v) || !isfinite(wv) || !isfinite(s.pos.c[c][i])) atomicOr(s.status, 1u);

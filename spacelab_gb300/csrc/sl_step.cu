@@ -50,6 +50,16 @@ __global__ void __launch_bounds__(256) drift_kernel(const __grid_constant__ Syst
         s.prev.c[c][i] = p;            // positions the pair distances of
         s.pos.c[c][i] = p + vh * dt;   // the previous step were taken at; :90
     }
+    if (s.f_pos[0]) {  // mixed form: scaled positions as double-float hi + lo
+        const double scale = ldexp(1.0, s.len_shift);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const double p = s.pos.c[c][i];
+            const float hi = d2f_bits(p, s.len_shift);
+            s.f_pos[c][i] = hi;
+            s.f_pos[3 + c][i] = d2f_bits(p - f2d_bits(hi) * scale, s.len_shift);
+        }
+    }
 }
 
 // ---------------------------------------------------------------- pass 2 --
@@ -356,7 +366,9 @@ __global__ void derive_kernel(const __grid_constant__ System s)
     s.rm[i] = recip_of(m);
     s.inv_moi[i] = 1.0 / moi;
     if (s.f_R) {  // mixed-precision form: FP32 constants, lengths scaled by 2^-len_shift
-        s.f_R[i] = d2f_bits(R, s.len_shift);
+        const float rh = d2f_bits(R, s.len_shift);
+        s.f_R[i] = rh;
+        s.f_Rlo[i] = d2f_bits(R - f2d_bits(rh) * ldexp(1.0, s.len_shift), s.len_shift);
         s.f_inv_m[i] = d2f_bits(1.0 / m, 0);
         s.f_inv_moi[i] = d2f_bits(1.0 / moi, 0);
     }

@@ -1,25 +1,27 @@
 // sl_step_mixed.cu -- the mixed-precision form of the step (SL_MODE_MIXED).
 //
-// FP64 is kept where precision is set:
-//   * positions and the whole integration (drift_kernel, shared with the
-//     exact form; pass 3 in mixed_rowsum_kernel);
-//   * the pair subtraction r = pos[B] - pos[A], |r|^2 and the squared gap
+// More than FP32 is kept where precision is set:
+//   * FP64: positions and the whole integration (drift_kernel, shared with
+//     the exact form; pass 3 in the row sums), the previous-step distance
+//     test that chooses kin or kout, the write-step potential energy per
+//     pair and the energy totals;
+//   * double-float (hi + lo FP32 pairs, ~48 significant bits, sl_df.cuh):
+//     the pair subtraction r = pos[B] - pos[A] from double-float copies of
+//     the scaled positions, |r|^2 and the squared gap
 //     g = (R_A + R_B)^2 - |r|^2, from which the overlap is taken as
-//     g / (R_A + R_B + |r|) -- no cancellation in R_A + R_B - |r|;
-//   * the previous-step distance test that chooses kin or kout;
-//   * per-sphere force and torque accumulation: each sphere's FP32 pair
-//     terms are added into an FP64 sum in ascending partner order;
-//   * the write-step potential energy per pair and the energy totals.
+//     g / (R_A + R_B + |r|) -- no cancellation in R_A + R_B - |r|; and the
+//     per-sphere sums of the FP32 pair terms (compensated, in ascending
+//     partner order, then converted to FP64).
 // Everything else -- distances, the vdW coefficient, elastic, gravity,
 // sliding and rolling friction, torques -- is FP32 on lengths scaled by
 // 2^-len_shift (about one radius), which keeps R^6 / (S^2 T^2) far from
-// FP32's range limits.  Float <-> double conversions are bit manipulation
-// on the integer pipe (f2d_bits / d2f_bits), so the FP64 pipe carries only
-// 8 operations per pair in the pair pass and 6 in the sums.
+// FP32's range limits.  The non-contact pair path thus issues no FP64
+// instruction: GB300's FP32 pipe is ~72x its FP64 pipe.
 // The physics follows ColliderSingleCore.cpp:104-253 term by term; only the
 // arithmetic and the evaluation order differ.
 #include "sl_device.cuh"
 #include "sl_kernels.h"
+#include "sl_df.cuh"
 #include "sl_pair_mixed.cuh"
 
 namespace sl {
@@ -27,9 +29,19 @@ namespace sl {
 namespace {
 
 struct ABlockMixed {
-    double x[kBlock], y[kBlock], z[kBlock], R[kBlock];
-    float Rs[kBlock], inv_m[kBlock];
+    float p[6][kBlock];  // scaled position hi (x, y, z), then lo (x, y, z)
+    float Rs[kBlock], Rlo[kBlock], inv_m[kBlock];
 };
+
+// |pos[B] - pos[A]|^2 in FP64, the formula of the previous-step distance in
+// contact_mixed (rare paths: the contact test, write-step energies).
+__device__ __forceinline__ double fp64_d2(const System& s, int A, int B)
+{
+    const double rx = s.pos.c[0][B] - s.pos.c[0][A];
+    const double ry = s.pos.c[1][B] - s.pos.c[1][A];
+    const double rz = s.pos.c[2][B] - s.pos.c[2][A];
+    return fma(rx, rx, fma(ry, ry, rz * rz));
+}
 
 // Same tiling as pair_tile_kernel: one warp per lower-triangular 32x32 block
 // tile, lane b = sphere 32Y+b, loop over the A block; terms stored as FP32
@@ -55,14 +67,17 @@ __global__ void __launch_bounds__(128, 4) mixed_pair_kernel(const __grid_constan
         tile_coords(t, X, Y);
         {
             const int i = X * kBlock + lane;
-            ab.x[lane] = s.pos.c[0][i]; ab.y[lane] = s.pos.c[1][i]; ab.z[lane] = s.pos.c[2][i];
-            ab.R[lane] = s.R[i]; ab.Rs[lane] = s.f_R[i]; ab.inv_m[lane] = s.f_inv_m[i];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) ab.p[k][lane] = s.f_pos[k][i];
+            ab.Rs[lane] = s.f_R[i]; ab.Rlo[lane] = s.f_Rlo[i]; ab.inv_m[lane] = s.f_inv_m[i];
         }
         __syncwarp();
         const int B = Y * kBlock + lane;
         const bool bvalid = B < s.n;
-        const double bx = s.pos.c[0][B], by = s.pos.c[1][B], bz = s.pos.c[2][B], Rb = s.R[B];
-        const float Rbs = s.f_R[B], inv_mb = s.f_inv_m[B];
+        float bp[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) bp[k] = s.f_pos[k][B];
+        const float Rbs = s.f_R[B], Rblo = s.f_Rlo[B], inv_mb = s.f_inv_m[B];
         const int a_end = min(kBlock, s.n - X * kBlock);
         double pe = 0;
         uint32_t rowbits = 0, colbits = 0;
@@ -73,38 +88,49 @@ __global__ void __launch_bounds__(128, 4) mixed_pair_kernel(const __grid_constan
             bool contact = false;
             if (valid) {
                 const int A = X * kBlock + a;
-                // FP64: subtraction, |r|^2, squared gap
-                const double rx = bx - ab.x[a], ry = by - ab.y[a], rz = bz - ab.z[a];
-                const double d2 = fma(rx, rx, fma(ry, ry, rz * rz));
-                const double sum = ab.R[a] + Rb;
-                const double gap2 = fma(sum, sum, -d2);
+                // double-float (~48 bits, FP32 pipe): subtraction, |r|^2 and
+                // the squared gap g = (R_A + R_B)^2 - |r|^2, in scaled lengths
+                const df::F2 rx = df::sub({bp[0], bp[3]}, {ab.p[0][a], ab.p[3][a]});
+                const df::F2 ry = df::sub({bp[1], bp[4]}, {ab.p[1][a], ab.p[4][a]});
+                const df::F2 rz = df::sub({bp[2], bp[5]}, {ab.p[2][a], ab.p[5][a]});
+                const df::F2 d2 = df::add(df::add(df::sqr(rx), df::sqr(ry)), df::sqr(rz));
+                const float Ras = ab.Rs[a];
+                const df::F2 sum = df::add({Ras, ab.Rlo[a]}, {Rbs, Rblo});
+                const df::F2 gap2 = df::sub(df::sqr(sum), d2);
                 // FP32 (scaled lengths)
-                const float rxs = d2f_bits(rx, sh), rys = d2f_bits(ry, sh), rzs = d2f_bits(rz, sh);
-                const float d2s = d2f_bits(d2, 2 * sh);
+                const float rxs = rx.hi, rys = ry.hi, rzs = rz.hi;
+                const float d2s = d2.hi;
                 const float inv_d = rsqrtf(d2s);
                 const float dist_s = d2s * inv_d;
-                const float Ras = ab.Rs[a];
-                const float ovl_s = __fdividef(d2f_bits(gap2, 2 * sh), Ras + Rbs + dist_s);
+                const float ovl_s = __fdividef(gap2.hi, Ras + Rbs + dist_s);
                 const float nx = rxs * inv_d, ny = rys * inv_d, nz = rzs * inv_d;
                 float fx, fy, fz;
-                // gap2 > 0 on the bit pattern (integer pipe); NaN excluded
-                const long long gb = __double_as_longlong(gap2);
-                if (gb > 0 && gb <= 0x7ff0000000000000ll) {
+                if (gap2.hi > 0.0f || (gap2.hi == 0.0f && gap2.lo > 0.0f)) {
                     contact = true;
                     const ContactIn in = gather_contact(s, A, B);
-                    const ContactF o = contact_mixed(in, s.mat, sh, d2, nx, ny, nz, dist_s * L, ovl_s * L, Ras, Rbs);
+                    // the kin/kout test compares |r|^2 with the previous step's,
+                    // both in FP64 from the FP64 positions with one formula
+                    const double d2_64 = fp64_d2(s, A, B);
+                    const ContactF o = contact_mixed(in, s.mat, sh, d2_64, nx, ny, nz, dist_s * L, ovl_s * L, Ras,
+                                                     Rbs);
                     fx = o.fx; fy = o.fy; fz = o.fz;
                     const float ima = s.f_inv_moi[A], imb = s.f_inv_moi[B];
                     float* ta = tbuf + (size_t)A * s.npad + B;
                     float* tb = tbuf + (size_t)B * s.npad + A;
                     ta[0] = o.tax * ima; ta[plane] = o.tay * ima; ta[2 * plane] = o.taz * ima;
                     tb[0] = o.tbx * imb; tb[plane] = o.tby * imb; tb[2 * plane] = o.tbz * imb;
-                    if (WRITE) pe += pair_pe_fp64(s.mat, ab.R[a], Rb, gap2, d2, true, o.k);
+                    if (WRITE) {
+                        const double sum64 = s.R[A] + s.R[B];
+                        pe += pair_pe_fp64(s.mat, s.R[A], s.R[B], fma(sum64, sum64, -d2_64), d2_64, true, o.k);
+                    }
                 } else {
                     const float h = fmaxf(-ovl_s, hmin_s);                  // :211-215
                     const float f = c_vdw * vdw_shape(h, Ras, Rbs);
                     fx = f * nx; fy = f * ny; fz = f * nz;
-                    if (WRITE) pe += pair_pe_fp64(s.mat, ab.R[a], Rb, gap2, d2, false, 0.0);
+                    if (WRITE) {  // write steps only: the FP64 geometry, as the contact branch
+                        const double d2_64 = fp64_d2(s, A, B), sum64 = s.R[A] + s.R[B];
+                        pe += pair_pe_fp64(s.mat, s.R[A], s.R[B], fma(sum64, sum64, -d2_64), d2_64, false, 0.0);
+                    }
                 }
                 const float ima = ab.inv_m[a];
                 float* pa = rowA + (size_t)a * s.npad;
