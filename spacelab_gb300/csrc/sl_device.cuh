@@ -60,6 +60,10 @@ struct System {
     // of the scaled positions (x, y, z hi, then x, y, z lo), the latter
     // written by the drift kernel every step
     float *f_Rlo, *f_pos[6];
+    // the mixed form's B-side pair terms [3][npad][npad] (FP32): pT[c][A][B]
+    // is sphere B's term from partner A, written coalesced; it is the upper
+    // half of pairbuf, whose FP32 view the A-side terms fill only in part
+    float* pairT;
     int len_shift;
 };
 

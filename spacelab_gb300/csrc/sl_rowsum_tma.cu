@@ -1,6 +1,7 @@
 // sl_rowsum_tma.cu -- the ordered row sums (pass 2's accumulation, then
-// pass 3) with the pair-term rows streamed into shared memory by TMA, for
-// FP64 terms (exact form) and FP32 terms summed in FP64 (mixed form).
+// pass 3) with the pair-term rows streamed into shared memory by TMA:
+// rowsum_tma_kernel for the exact form's FP64 terms, rowsum_mixed_kernel for
+// the mixed form's FP32 terms (A-side rows and B-side columns, see there).
 //
 // Thread (c, i) adds acc_c[i] = sum over partners j ascending of
 // pairbuf[c][i][j] -- the order in which the reference adds terms to acc[i]
@@ -8,7 +9,7 @@
 // blocks [b0, b1), continuing the running sums kept in acc/aacc between
 // segments; the last segment does pass 3 (:263-267).  FP64 terms are added
 // in FP64 (the reference's own additions); the mixed form's FP32 terms are
-// added in a compensated double-float sum on the FP32 pipe.
+// added in a compensated double-float sum on the FP32 pipe (sl_df.cuh).
 //
 // Layout: one warp per (component, 32-row block), lane = row, kRsWarps
 // independent warps per CTA so that the warps and their FP64 add chains
@@ -82,28 +83,9 @@ struct RsTerm<double> {
 };
 
 template <>
-struct RsTerm<float> {
+struct RsTerm<float> {  // the mixed form's buffers (rowsum_mixed_kernel)
     static constexpr int kBoxCols = 32;
     static constexpr CUtensorMapDataType kType = CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
-    // compensated FP32 running sum (double-float, sl_df.cuh) on the FP32
-    // pipe, in ascending partner order; converted to FP64 at the end
-    struct Acc {
-        df::Sum a;
-        __device__ void start(double x)
-        {
-            const float h = d2f_bits(x, 0);
-            a = {h, d2f_bits(x - f2d_bits(h), 0)};
-        }
-        __device__ void add_chunk(const uint4& u)
-        {
-            a.add(__uint_as_float(u.x));
-            a.add(__uint_as_float(u.y));
-            a.add(__uint_as_float(u.z));
-            a.add(__uint_as_float(u.w));
-        }
-        __device__ void add_term(float x) { a.add(x); }
-        __device__ double value() const { return f2d_bits(a.s) + f2d_bits(a.c); }
-    };
 };
 
 template <typename T, int BPS>
@@ -236,6 +218,132 @@ __global__ void __launch_bounds__(32 * kRsWarps, 8 / BPS) rowsum_tma_kernel(cons
     if (!isfinite(v) || !isfinite(wv) || !isfinite(s.pos.c[c][i])) atomicOr(s.status, 1u);
 }
 
+// ---------------------------------------------------------------------------
+// Mixed form.  Row i's FP32 terms for partners j < i (i is the A sphere) are
+// in the A-side buffer pA[c][i][j], row-major; for j > i (i is B) in the
+// B-side buffer pT[c][j][i], which the mixed pair kernel writes coalesced
+// (its lanes run over B).  Stage q of row block I is partner block q read
+// as rows of pA for q <= I (on the diagonal block the entries j >= i are
+// never written and hold +0.0), and partner block q-1 read as columns of pT
+// for q > I (on the diagonal the entries j <= i hold +0.0).  Adding every
+// entry of every stage therefore adds the terms in ascending j.
+__device__ __forceinline__ void rs_rows(const unsigned char* stage, int lane, float (&v)[kBlock])
+{
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const uint4 u = rs_chunk(stage, lane, k);
+        v[4 * k] = __uint_as_float(u.x);
+        v[4 * k + 1] = __uint_as_float(u.y);
+        v[4 * k + 2] = __uint_as_float(u.z);
+        v[4 * k + 3] = __uint_as_float(u.w);
+    }
+}
+
+// column `lane` of a swizzled 32 x 32 float box: at each row the lanes' 4-byte
+// reads cover the row's 128 bytes once (no bank conflict)
+__device__ __forceinline__ void rs_cols(const unsigned char* stage, int lane, float (&v)[kBlock])
+{
+#pragma unroll
+    for (int a = 0; a < kBlock; ++a)
+        v[a] = *reinterpret_cast<const float*>(stage + a * 128 + ((((lane >> 2) ^ (a & 7)) << 4) | ((lane & 3) << 2)));
+}
+
+__global__ void __launch_bounds__(32 * kRsWarps, 8) rowsum_mixed_kernel(const __grid_constant__ System s,
+                                                                        const __grid_constant__ CUtensorMap mapA,
+                                                                        const __grid_constant__ CUtensorMap mapT)
+{
+    using Stage = RsStage<1>;
+    extern __shared__ unsigned char rs_raw[];
+    __shared__ __align__(8) uint64_t full_all[kRsWarps][kRsStages];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int wg = blockIdx.x * kRsWarps + warp;
+    if (wg >= 3 * s.nb) return;  // no block-wide synchronisation below
+    unsigned char* buf = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(rs_raw) + 1023) &
+                                                          ~static_cast<uintptr_t>(1023)) +
+                         warp * Stage::kWarpBytes;
+    uint64_t* full = full_all[warp];
+    const int c = wg / s.nb;
+    const int rb = wg - c * s.nb;
+    const int i = rb * kBlock + lane;  // < npad
+    const int nq = s.nb + 1;
+    auto issue = [&](int q) {
+        const int st = q % kRsStages;
+        tma::mbar_arrive_expect_tx(&full[st], kRsBox);
+        if (q <= rb)
+            tma::load_2d(buf + st * kRsBox, &mapA, q * kBlock, c * s.npad + rb * kBlock, &full[st]);
+        else
+            tma::load_2d(buf + st * kRsBox, &mapT, rb * kBlock, c * s.npad + (q - 1) * kBlock, &full[st]);
+    };
+    if (lane == 0) {
+        for (int k = 0; k < kRsStages; ++k) tma::mbar_init(&full[k], 1);
+        tma::fence_barrier_init();
+        for (int q = 0; q < nq && q < kRsStages; ++q) issue(q);
+    }
+    __syncwarp();
+
+    df::Sum acc{0.0f, 0.0f}, aacc{0.0f, 0.0f};
+    const size_t plane = (size_t)s.npad * s.npad;
+    const uint32_t* mrow = s.cmask + (size_t)i * s.nb;  // rows < npad exist; padding rows are 0
+    const float* trow = reinterpret_cast<const float*>(s.torqbuf) + c * plane + (size_t)i * s.npad;
+    uint32_t wnext = mrow[0];
+    float cur[kBlock], nxt[kBlock];
+    int waited = 0;  // first stage not yet observed complete
+    bool ok = __all_sync(0xffffffffu, tma::mbar_wait(&full[0], 0));
+    if (ok) {
+        rs_rows(buf, lane, cur);  // stage 0 is always A-side rows
+        waited = 1;
+    }
+    for (int q = 0; ok && q < nq; ++q) {
+        __syncwarp();  // every lane has stage q in registers: its buffer is free
+        if (lane == 0 && q + kRsStages < nq) {
+            tma::fence_proxy_async();
+            issue(q + kRsStages);
+        }
+        if (q + 1 < nq) {
+            const int st1 = (q + 1) % kRsStages;
+            ok = __all_sync(0xffffffffu, tma::mbar_wait(&full[st1], ((q + 1) / kRsStages) & 1));
+            if (ok) {
+                if (q + 1 <= rb)
+                    rs_rows(buf + st1 * kRsBox, lane, nxt);
+                else
+                    rs_cols(buf + st1 * kRsBox, lane, nxt);
+                waited = q + 2;
+            }
+        }
+#pragma unroll
+        for (int a = 0; a < kBlock; ++a) acc.add(cur[a]);
+        if (q != rb) {  // partner block J complete (the diagonal after its B part): torque terms
+            const int J = q < rb ? q : q - 1;
+            uint32_t wd = wnext;
+            if (J + 1 < s.nb) wnext = mrow[J + 1];
+            while (wd) {
+                const int bit = __ffs(wd) - 1;
+                wd &= wd - 1;
+                aacc.add(trow[J * kBlock + bit]);
+            }
+        }
+#pragma unroll
+        for (int a = 0; a < kBlock; ++a) cur[a] = nxt[a];
+    }
+    if (!ok) {
+        const int issued = min(nq, waited + kRsStages);
+        for (int qq = waited; qq < issued; ++qq) tma::mbar_wait(&full[qq % kRsStages], (qq / kRsStages) & 1);
+        if (lane == 0) atomicOr(s.status, kStatusWaitTimeoutBit);
+        return;
+    }
+    if (i >= s.n) return;
+    const double fa = f2d_bits(acc.s) + f2d_bits(acc.c), ta = f2d_bits(aacc.s) + f2d_bits(aacc.c);
+    s.acc.c[c][i] = fa;
+    s.aacc.c[c][i] = ta;
+    const double dt = s.sc->dt;
+    const double v = s.velh.c[c][i] + (.5 * fa) * dt;
+    const double wv = s.wh.c[c][i] + (.5 * ta) * dt;
+    s.vel.c[c][i] = v;
+    s.w.c[c][i] = wv;
+    if (!isfinite(v) || !isfinite(wv) || !isfinite(s.pos.c[c][i])) atomicOr(s.status, 1u);
+}
+
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
 {
     static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
@@ -254,29 +362,38 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
 // The pair-term buffer [3][npad][npad] as a 2D tensor of 3 npad rows of npad
 // columns; boxes of 128 bytes x 32 rows with the 128-byte swizzle.
 template <typename T>
-bool make_map(const System& s, CUtensorMap* map)
+bool make_map(const System& s, void* base, CUtensorMap* map)
 {
     PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
-    if (!encode || !s.pairbuf) return false;
+    if (!encode || !base) return false;
     const cuuint64_t dims[2] = {(cuuint64_t)s.npad, (cuuint64_t)3 * s.npad};
     const cuuint64_t strides[1] = {(cuuint64_t)s.npad * sizeof(T)};
     const cuuint32_t box[2] = {(cuuint32_t)RsTerm<T>::kBoxCols, (cuuint32_t)kBlock};
     const cuuint32_t estr[2] = {1, 1};
-    if (encode(map, RsTerm<T>::kType, 2, s.pairbuf, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-               CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) !=
-        CUDA_SUCCESS)
-        return false;
-    return cudaFuncSetAttribute(rowsum_tma_kernel<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                RsStage<1>::kSmem) == cudaSuccess &&
-           cudaFuncSetAttribute(rowsum_tma_kernel<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                RsStage<2>::kSmem) == cudaSuccess;
+    return encode(map, RsTerm<T>::kType, 2, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 }  // namespace
 
-bool make_pair_map(const System& s, bool fp32_terms, CUtensorMap* map)
+bool make_pair_map(const System& s, bool fp32_terms, CUtensorMap* map, CUtensorMap* mapT)
 {
-    return fp32_terms ? make_map<float>(s, map) : make_map<double>(s, map);
+    if (!fp32_terms)
+        return make_map<double>(s, s.pairbuf, map) &&
+               cudaFuncSetAttribute(rowsum_tma_kernel<double, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    RsStage<1>::kSmem) == cudaSuccess &&
+               cudaFuncSetAttribute(rowsum_tma_kernel<double, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    RsStage<2>::kSmem) == cudaSuccess;
+    return make_map<float>(s, s.pairbuf, map) && make_map<float>(s, s.pairT, mapT) &&
+           cudaFuncSetAttribute(rowsum_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                RsStage<1>::kSmem) == cudaSuccess;
+}
+
+void launch_rowsum_mixed(const System& s, const CUtensorMap& mapA, const CUtensorMap& mapT, cudaStream_t st)
+{
+    rowsum_mixed_kernel<<<(3 * s.nb + kRsWarps - 1) / kRsWarps, 32 * kRsWarps, RsStage<1>::kSmem, st>>>(s, mapA,
+                                                                                                       mapT);
 }
 
 template <typename T>
@@ -294,6 +411,5 @@ void launch_rowsum_tma(const System& s, const CUtensorMap& map, int b0, int b1, 
 }
 
 template void launch_rowsum_tma<double>(const System&, const CUtensorMap&, int, int, int, int, int, cudaStream_t);
-template void launch_rowsum_tma<float>(const System&, const CUtensorMap&, int, int, int, int, int, cudaStream_t);
 
 }  // namespace sl

@@ -44,8 +44,11 @@ __device__ __forceinline__ double fp64_d2(const System& s, int A, int B)
 }
 
 // Same tiling as pair_tile_kernel: one warp per lower-triangular 32x32 block
-// tile, lane b = sphere 32Y+b, loop over the A block; terms stored as FP32
-// in the [3][npad][npad] float view of pairbuf/torqbuf.
+// tile, lane b = sphere 32Y+b, loop over the A block; terms stored as FP32:
+// sphere A's in the A-side buffer pA[c][A][B] (the float view of pairbuf),
+// sphere B's in the B-side buffer pairT[c][A][B] -- both indexed by (A, B),
+// so that both stores of a warp are coalesced over B.  Torques (contacts
+// only) go to the float view of torqbuf, [A][B] and [B][A].
 template <bool WRITE>
 __global__ void __launch_bounds__(128, 4) mixed_pair_kernel(const __grid_constant__ System s)
 {
@@ -81,8 +84,8 @@ __global__ void __launch_bounds__(128, 4) mixed_pair_kernel(const __grid_constan
         const int a_end = min(kBlock, s.n - X * kBlock);
         double pe = 0;
         uint32_t rowbits = 0, colbits = 0;
-        float* rowA = pbuf + (size_t)(X * kBlock) * s.npad + B;
-        float* rowB = pbuf + (size_t)B * s.npad + X * kBlock;
+        float* rowA = pbuf + (size_t)(X * kBlock) * s.npad + B;      // + a npad: A-side term of row A
+        float* rowAT = s.pairT + (size_t)(X * kBlock) * s.npad + B;  // + a npad: B-side term, coalesced
         for (int a = 0; a < a_end; ++a) {
             const bool valid = bvalid && (X != Y || lane < a);
             bool contact = false;
@@ -135,7 +138,7 @@ __global__ void __launch_bounds__(128, 4) mixed_pair_kernel(const __grid_constan
                 const float ima = ab.inv_m[a];
                 float* pa = rowA + (size_t)a * s.npad;
                 __stcs(pa, fx * ima); __stcs(pa + plane, fy * ima); __stcs(pa + 2 * plane, fz * ima);
-                float* pb = rowB + a;
+                float* pb = rowAT + (size_t)a * s.npad;
                 __stcs(pb, -fx * inv_mb); __stcs(pb + plane, -fy * inv_mb); __stcs(pb + 2 * plane, -fz * inv_mb);
             }
             const uint32_t bal = __ballot_sync(0xffffffffu, contact);
@@ -156,11 +159,11 @@ __global__ void __launch_bounds__(128, 4) mixed_pair_kernel(const __grid_constan
     }
 }
 
-constexpr int kMixBatch = 8;  // float4 loads in flight per thread
 constexpr int kMixThreads = 32;
 
-// Thread (c, i): FP64 sum of the FP32 terms of row i in ascending partner
-// order, torque terms of contact partners likewise, then pass 3 in FP64.
+// Plain-load form of the row sums (used only when no tensor map could be
+// made): thread (c, i) sums the FP32 terms of sphere i in FP64 in ascending
+// partner order, torque terms of contact partners likewise, then pass 3.
 __global__ void __launch_bounds__(kMixThreads) mixed_rowsum_kernel(const __grid_constant__ System s)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -169,31 +172,12 @@ __global__ void __launch_bounds__(kMixThreads) mixed_rowsum_kernel(const __grid_
     const int i = t - c * s.n;
     const int n = s.n;
     const size_t plane = (size_t)s.npad * s.npad;
-    const float* rowf = reinterpret_cast<const float*>(s.pairbuf) + c * plane + (size_t)i * s.npad;
-    const float4* row = reinterpret_cast<const float4*>(rowf);
-    const int nv = (n + 3) / 4;
-    float4 cur[kMixBatch], nxt[kMixBatch];
-    const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-    for (int k = 0; k < kMixBatch; ++k) cur[k] = k < nv ? __ldcs(row + k) : zero4;
+    // partners j < i from the A-side row i, j > i from the B-side column i
+    const float* rowA = reinterpret_cast<const float*>(s.pairbuf) + c * plane + (size_t)i * s.npad;
+    const float* colT = s.pairT + c * plane + i;
     double acc = 0.0;
-    for (int base = 0; base < nv; base += kMixBatch) {
-#pragma unroll
-        for (int k = 0; k < kMixBatch; ++k) {
-            const int q = base + kMixBatch + k;
-            nxt[k] = q < nv ? __ldcs(row + q) : zero4;
-        }
-#pragma unroll
-        for (int k = 0; k < kMixBatch; ++k) {
-            const int j = 4 * (base + k);
-            const float v[4] = {cur[k].x, cur[k].y, cur[k].z, cur[k].w};
-#pragma unroll
-            for (int u = 0; u < 4; ++u)
-                if (j + u < n && j + u != i) acc += f2d_bits(v[u]);
-        }
-#pragma unroll
-        for (int k = 0; k < kMixBatch; ++k) cur[k] = nxt[k];
-    }
+    for (int j = 0; j < i; ++j) acc += f2d_bits(__ldcs(rowA + j));
+    for (int j = i + 1; j < n; ++j) acc += f2d_bits(__ldcs(colT + (size_t)j * s.npad));
     double aacc = 0.0;
     const uint32_t* mrow = s.cmask + (size_t)i * s.nb;
     const float* trow = reinterpret_cast<const float*>(s.torqbuf) + c * plane + (size_t)i * s.npad;
@@ -218,7 +202,7 @@ __global__ void __launch_bounds__(kMixThreads) mixed_rowsum_kernel(const __grid_
 }  // namespace
 
 void launch_step_mixed(const System& s, bool write, int num_sms, cudaStream_t st, StepTimers* tm,
-                       const CUtensorMap* map)
+                       const CUtensorMap* map, const CUtensorMap* mapT)
 {
     launch_drift(s, st);
     if (tm) cudaEventRecord(tm->ev[0], st);
@@ -230,8 +214,8 @@ void launch_step_mixed(const System& s, bool write, int num_sms, cudaStream_t st
     else
         mixed_pair_kernel<false><<<pb, 128, 0, st>>>(s);
     if (tm) cudaEventRecord(tm->ev[1], st);
-    if (map)
-        launch_rowsum_tma<float>(s, *map, 0, s.nb, 1, 1, num_sms, st);
+    if (map && mapT)
+        launch_rowsum_mixed(s, *map, *mapT, st);
     else
         mixed_rowsum_kernel<<<(3 * s.n + kMixThreads - 1) / kMixThreads, kMixThreads, 0, st>>>(s);
     if (tm) cudaEventRecord(tm->ev[2], st);
