@@ -43,7 +43,8 @@ void launch_step(const System& s, bool write, int num_sms, cudaStream_t st, Step
 // then).
 bool make_pair_map(const System& s, bool fp32_terms, CUtensorMap* map, CUtensorMap* mapT);
 // The mixed form's row sums: A-side rows (mapA) and B-side columns (mapT).
-void launch_rowsum_mixed(const System& s, const CUtensorMap& mapA, const CUtensorMap& mapT, cudaStream_t st);
+void launch_rowsum_mixed(const System& s, const CUtensorMap& mapA, const CUtensorMap& mapT, int num_sms,
+                         cudaStream_t st);
 // The TMA-streamed ordered row sums over partner blocks [b0, b1) with terms
 // of type T (double: exact form, float: mixed form); first/last as for the
 // plain row sums.

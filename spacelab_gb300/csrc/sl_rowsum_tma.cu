@@ -225,8 +225,10 @@ __global__ void __launch_bounds__(32 * kRsWarps, 8 / BPS) rowsum_tma_kernel(cons
 // (its lanes run over B).  Stage q of row block I is partner block q read
 // as rows of pA for q <= I (on the diagonal block the entries j >= i are
 // never written and hold +0.0), and partner block q-1 read as columns of pT
-// for q > I (on the diagonal the entries j <= i hold +0.0).  Adding every
-// entry of every stage therefore adds the terms in ascending j.
+// for q > I (on the diagonal the entries j <= i hold +0.0).  Every entry of
+// every stage is added, in ascending j, into four interleaved compensated
+// sums (the mixed form is not bound to the reference's rounding sequence;
+// the sums are near exact either way).
 __device__ __forceinline__ void rs_rows(const unsigned char* stage, int lane, float (&v)[kBlock])
 {
 #pragma unroll
@@ -248,11 +250,25 @@ __device__ __forceinline__ void rs_cols(const unsigned char* stage, int lane, fl
         v[a] = *reinterpret_cast<const float*>(stage + a * 128 + ((((lane >> 2) ^ (a & 7)) << 4) | ((lane & 3) << 2)));
 }
 
-__global__ void __launch_bounds__(32 * kRsWarps, 8) rowsum_mixed_kernel(const __grid_constant__ System s,
-                                                                        const __grid_constant__ CUtensorMap mapA,
-                                                                        const __grid_constant__ CUtensorMap mapT)
+// NST stages of one box per warp: kRsStages when the system's warps are many
+// (16 warps share an SM), kMixDeepStages when they are few -- a stage holds
+// only ~150 cycles of adds here, so many copies must be in flight to cover
+// the TMA latency.
+constexpr int kMixDeepStages = 8;
+
+template <int NST>
+struct MixShape {
+    static constexpr int kWarpBytes = NST * kRsBox;
+    static constexpr int kSmem = kRsWarps * kWarpBytes + 1024;  // + alignment slack
+};
+
+template <int NST>
+__global__ void __launch_bounds__(32 * kRsWarps, NST == kRsStages ? 8 : 3)
+    rowsum_mixed_kernel(const __grid_constant__ System s, const __grid_constant__ CUtensorMap mapA,
+                        const __grid_constant__ CUtensorMap mapT)
 {
-    using Stage = RsStage<1>;
+    constexpr int kRsStages = NST;  // shadows the file-wide depth in this kernel
+    using Stage = MixShape<NST>;
     extern __shared__ unsigned char rs_raw[];
     __shared__ __align__(8) uint64_t full_all[kRsWarps][kRsStages];
     const int lane = threadIdx.x & 31;
@@ -282,11 +298,17 @@ __global__ void __launch_bounds__(32 * kRsWarps, 8) rowsum_mixed_kernel(const __
     }
     __syncwarp();
 
-    df::Sum acc{0.0f, 0.0f}, aacc{0.0f, 0.0f};
+    // four compensated sums (terms a = 0, 1, 2, 3 mod 4 of each block), so
+    // that a lane has four independent FP32 add chains in flight; their
+    // FP64 total is formed at the end
+    constexpr int kLanes = 4;
+    df::Sum acc[kLanes] = {}, aacc{0.0f, 0.0f};
     const size_t plane = (size_t)s.npad * s.npad;
     const uint32_t* mrow = s.cmask + (size_t)i * s.nb;  // rows < npad exist; padding rows are 0
     const float* trow = reinterpret_cast<const float*>(s.torqbuf) + c * plane + (size_t)i * s.npad;
-    uint32_t wnext = mrow[0];
+    // contact-mask words of partner blocks J .. J+3, loaded four blocks ahead
+    // (a stage's adds take too few cycles to cover a global load)
+    uint32_t w0 = mrow[0], w1 = s.nb > 1 ? mrow[1] : 0u, w2 = s.nb > 2 ? mrow[2] : 0u, w3 = s.nb > 3 ? mrow[3] : 0u;
     float cur[kBlock], nxt[kBlock];
     int waited = 0;  // first stage not yet observed complete
     bool ok = __all_sync(0xffffffffu, tma::mbar_wait(&full[0], 0));
@@ -312,11 +334,14 @@ __global__ void __launch_bounds__(32 * kRsWarps, 8) rowsum_mixed_kernel(const __
             }
         }
 #pragma unroll
-        for (int a = 0; a < kBlock; ++a) acc.add(cur[a]);
+        for (int a = 0; a < kBlock; ++a) acc[a % kLanes].add(cur[a]);
         if (q != rb) {  // partner block J complete (the diagonal after its B part): torque terms
             const int J = q < rb ? q : q - 1;
-            uint32_t wd = wnext;
-            if (J + 1 < s.nb) wnext = mrow[J + 1];
+            uint32_t wd = w0;
+            w0 = w1;
+            w1 = w2;
+            w2 = w3;
+            w3 = J + 4 < s.nb ? mrow[J + 4] : 0u;
             while (wd) {
                 const int bit = __ffs(wd) - 1;
                 wd &= wd - 1;
@@ -333,7 +358,10 @@ __global__ void __launch_bounds__(32 * kRsWarps, 8) rowsum_mixed_kernel(const __
         return;
     }
     if (i >= s.n) return;
-    const double fa = f2d_bits(acc.s) + f2d_bits(acc.c), ta = f2d_bits(aacc.s) + f2d_bits(aacc.c);
+    double fa = 0.0;
+#pragma unroll
+    for (int k = 0; k < kLanes; ++k) fa += f2d_bits(acc[k].s) + f2d_bits(acc[k].c);
+    const double ta = f2d_bits(aacc.s) + f2d_bits(aacc.c);
     s.acc.c[c][i] = fa;
     s.aacc.c[c][i] = ta;
     const double dt = s.sc->dt;
@@ -386,14 +414,21 @@ bool make_pair_map(const System& s, bool fp32_terms, CUtensorMap* map, CUtensorM
                cudaFuncSetAttribute(rowsum_tma_kernel<double, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     RsStage<2>::kSmem) == cudaSuccess;
     return make_map<float>(s, s.pairbuf, map) && make_map<float>(s, s.pairT, mapT) &&
-           cudaFuncSetAttribute(rowsum_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                RsStage<1>::kSmem) == cudaSuccess;
+           cudaFuncSetAttribute(rowsum_mixed_kernel<kRsStages>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                MixShape<kRsStages>::kSmem) == cudaSuccess &&
+           cudaFuncSetAttribute(rowsum_mixed_kernel<kMixDeepStages>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                MixShape<kMixDeepStages>::kSmem) == cudaSuccess;
 }
 
-void launch_rowsum_mixed(const System& s, const CUtensorMap& mapA, const CUtensorMap& mapT, cudaStream_t st)
+void launch_rowsum_mixed(const System& s, const CUtensorMap& mapA, const CUtensorMap& mapT, int num_sms,
+                         cudaStream_t st)
 {
-    rowsum_mixed_kernel<<<(3 * s.nb + kRsWarps - 1) / kRsWarps, 32 * kRsWarps, RsStage<1>::kSmem, st>>>(s, mapA,
-                                                                                                       mapT);
+    const int ctas = (3 * s.nb + kRsWarps - 1) / kRsWarps;
+    if (ctas <= 3 * num_sms)  // every warp fits at 3 deep CTAs per SM
+        rowsum_mixed_kernel<kMixDeepStages><<<ctas, 32 * kRsWarps, MixShape<kMixDeepStages>::kSmem, st>>>(s, mapA,
+                                                                                                          mapT);
+    else
+        rowsum_mixed_kernel<kRsStages><<<ctas, 32 * kRsWarps, MixShape<kRsStages>::kSmem, st>>>(s, mapA, mapT);
 }
 
 template <typename T>

@@ -215,7 +215,7 @@ void launch_step_mixed(const System& s, bool write, int num_sms, cudaStream_t st
         mixed_pair_kernel<false><<<pb, 128, 0, st>>>(s);
     if (tm) cudaEventRecord(tm->ev[1], st);
     if (map && mapT)
-        launch_rowsum_mixed(s, *map, *mapT, st);
+        launch_rowsum_mixed(s, *map, *mapT, num_sms, st);
     else
         mixed_rowsum_kernel<<<(3 * s.n + kMixThreads - 1) / kMixThreads, kMixThreads, 0, st>>>(s);
     if (tm) cudaEventRecord(tm->ev[2], st);
