@@ -61,9 +61,8 @@ struct sl_handle {
     cudaStream_t stream = nullptr;
     // exact mode: side stream + events overlapping row sums with pair phases
     sl::StepOverlap ov{};
-    CUtensorMap pair_map{};   // the pair-term buffer for the TMA row sums
-    CUtensorMap pair_mapT{};  // mixed form: its B-side buffer
-    bool has_map = false;
+    CUtensorMap pair_map{};  // exact form: the pair-term buffer for the TMA row sums
+    bool has_map = false;     // the bulk-copy row sums are ready
     bool has_ov = false;   // ov's stream and events exist
     bool overlap = false;  // steps use them
     void* arena = nullptr;
@@ -96,8 +95,7 @@ int check_handle(const sl_handle* h)
 void launch_mode_step(sl_handle* h, bool write, sl::StepTimers* tm)
 {
     if (h->mode == SL_MODE_MIXED)
-        sl::launch_step_mixed(h->sys, write, h->num_sms, h->stream, tm, h->has_map ? &h->pair_map : nullptr,
-                              h->has_map ? &h->pair_mapT : nullptr);
+        sl::launch_step_mixed(h->sys, write, h->num_sms, h->stream, tm, h->has_map);
     else
         sl::launch_step(h->sys, write, h->num_sms, h->stream, tm, h->overlap ? &h->ov : nullptr,
                         h->has_map ? &h->pair_map : nullptr);
@@ -258,7 +256,7 @@ int sl_create(int n, const sl_material* mat, int mode, sl_handle** out)
     h->d_sc = reinterpret_cast<sl::Scalars*>(base + o_scl);
     h->d_stage = reinterpret_cast<double*>(base + o_dstage);
     s.sc = h->d_sc;
-    h->has_map = sl::make_pair_map(s, mode == SL_MODE_MIXED, &h->pair_map, &h->pair_mapT);
+    h->has_map = sl::make_pair_map(s, mode == SL_MODE_MIXED, &h->pair_map);
     e = cudaMemsetAsync(h->arena, 0, h->arena_bytes, h->stream);
     if (e != cudaSuccess) { sl_destroy(h); return cuda_fail(e, "cudaMemset"); }
     e = cudaMallocHost(&h->staging, 18 * np * sizeof(double));

@@ -60,12 +60,24 @@ struct System {
     // of the scaled positions (x, y, z hi, then x, y, z lo), the latter
     // written by the drift kernel every step
     float *f_Rlo, *f_pos[6];
-    // the mixed form's B-side pair terms [3][npad][npad] (FP32): pT[c][A][B]
-    // is sphere B's term from partner A, written coalesced; it is the upper
-    // half of pairbuf, whose FP32 view the A-side terms fill only in part
+    // the mixed form's B-side pair terms (FP32): sphere B's term from partner
+    // A, at mixed_term_index(A, B); it is the upper half of pairbuf, whose
+    // FP32 view the A-side terms fill only in part
     float* pairT;
     int len_shift;
 };
+
+// The mixed form's pair-term layout (A side in the FP32 view of pairbuf, B
+// side in pairT, each [3] planes of npad^2 floats): tile-major, 32 x 32
+// tiles of 4 KB stored contiguously, tile (I, J) at (I nb + J) * 1024, and
+// inside a tile row a's 16-byte chunks permuted by XOR with (a & 7) -- the
+// 128-byte swizzle -- so that a tile copied to shared memory as one block
+// can be read by rows or by columns without bank conflicts.
+__device__ __forceinline__ size_t mixed_term_index(int nb, int A, int B)
+{
+    const int a = A & 31, b = B & 31;
+    return ((size_t)(A >> 5) * nb + (B >> 5)) * 1024 + a * 32 + ((((b >> 2) ^ (a & 7)) << 2) | (b & 3));
+}
 
 // Operands of a pair's contact branch beyond positions and radii (the
 // contact branch is rare: O(N) of the O(N^2) pairs, so they are gathered

@@ -1,7 +1,8 @@
 // sl_rowsum_tma.cu -- the ordered row sums (pass 2's accumulation, then
-// pass 3) with the pair-term rows streamed into shared memory by TMA:
-// rowsum_tma_kernel for the exact form's FP64 terms, rowsum_mixed_kernel for
-// the mixed form's FP32 terms (A-side rows and B-side columns, see there).
+// pass 3) with the pair terms streamed into shared memory by the bulk-copy
+// (TMA) engine: rowsum_tma_kernel for the exact form's FP64 terms (tensor-
+// map boxes of row-major rows), rowsum_mixed_kernel for the mixed form's
+// FP32 terms (whole tiles, A-side rows and B-side columns, see there).
 //
 // Thread (c, i) adds acc_c[i] = sum over partners j ascending of
 // pairbuf[c][i][j] -- the order in which the reference adds terms to acc[i]
@@ -80,12 +81,6 @@ struct RsTerm<double> {
         __device__ void add_term(double x) { a += x; }
         __device__ double value() const { return a; }
     };
-};
-
-template <>
-struct RsTerm<float> {  // the mixed form's buffers (rowsum_mixed_kernel)
-    static constexpr int kBoxCols = 32;
-    static constexpr CUtensorMapDataType kType = CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
 };
 
 template <typename T, int BPS>
@@ -220,12 +215,12 @@ __global__ void __launch_bounds__(32 * kRsWarps, 8 / BPS) rowsum_tma_kernel(cons
 
 // ---------------------------------------------------------------------------
 // Mixed form.  Row i's FP32 terms for partners j < i (i is the A sphere) are
-// in the A-side buffer pA[c][i][j], row-major; for j > i (i is B) in the
-// B-side buffer pT[c][j][i], which the mixed pair kernel writes coalesced
-// (its lanes run over B).  Stage q of row block I is partner block q read
-// as rows of pA for q <= I (on the diagonal block the entries j >= i are
-// never written and hold +0.0), and partner block q-1 read as columns of pT
-// for q > I (on the diagonal the entries j <= i hold +0.0).  Every entry of
+// the A-side entries (i, j); for j > i (i is B) the B-side entries (j, i),
+// both in the tile-major swizzled layout of mixed_term_index, so that one
+// bulk copy brings a whole 32 x 32 tile.  Stage q of row block I is A-side
+// tile (I, q) read by rows for q <= I (on the diagonal tile the entries
+// j >= i are never written and hold +0.0), and B-side tile (q-1, I) read by
+// columns for q > I (on the diagonal the entries j <= i hold +0.0).  Every entry of
 // every stage is added, in ascending j, into four interleaved compensated
 // sums (the mixed form is not bound to the reference's rounding sequence;
 // the sums are near exact either way).
@@ -264,8 +259,7 @@ struct MixShape {
 
 template <int NST>
 __global__ void __launch_bounds__(32 * kRsWarps, NST == kRsStages ? 8 : 3)
-    rowsum_mixed_kernel(const __grid_constant__ System s, const __grid_constant__ CUtensorMap mapA,
-                        const __grid_constant__ CUtensorMap mapT)
+    rowsum_mixed_kernel(const __grid_constant__ System s)
 {
     constexpr int kRsStages = NST;  // shadows the file-wide depth in this kernel
     using Stage = MixShape<NST>;
@@ -283,13 +277,16 @@ __global__ void __launch_bounds__(32 * kRsWarps, NST == kRsStages ? 8 : 3)
     const int rb = wg - c * s.nb;
     const int i = rb * kBlock + lane;  // < npad
     const int nq = s.nb + 1;
+    const size_t plane = (size_t)s.npad * s.npad;
+    const float* pA = reinterpret_cast<const float*>(s.pairbuf) + c * plane;
+    const float* pT = s.pairT + c * plane;
+    // stage q: A-side tile (I, q) for q <= I, B-side tile (q - 1, I) after;
+    // each is 4 KB of contiguous memory (mixed_term_index), one bulk copy
     auto issue = [&](int q) {
         const int st = q % kRsStages;
+        const float* src = q <= rb ? pA + ((size_t)rb * s.nb + q) * 1024 : pT + ((size_t)(q - 1) * s.nb + rb) * 1024;
         tma::mbar_arrive_expect_tx(&full[st], kRsBox);
-        if (q <= rb)
-            tma::load_2d(buf + st * kRsBox, &mapA, q * kBlock, c * s.npad + rb * kBlock, &full[st]);
-        else
-            tma::load_2d(buf + st * kRsBox, &mapT, rb * kBlock, c * s.npad + (q - 1) * kBlock, &full[st]);
+        tma::load_1d(buf + st * kRsBox, src, kRsBox, &full[st]);
     };
     if (lane == 0) {
         for (int k = 0; k < kRsStages; ++k) tma::mbar_init(&full[k], 1);
@@ -303,7 +300,6 @@ __global__ void __launch_bounds__(32 * kRsWarps, NST == kRsStages ? 8 : 3)
     // FP64 total is formed at the end
     constexpr int kLanes = 4;
     df::Sum acc[kLanes] = {}, aacc{0.0f, 0.0f};
-    const size_t plane = (size_t)s.npad * s.npad;
     const uint32_t* mrow = s.cmask + (size_t)i * s.nb;  // rows < npad exist; padding rows are 0
     const float* trow = reinterpret_cast<const float*>(s.torqbuf) + c * plane + (size_t)i * s.npad;
     // contact-mask words of partner blocks J .. J+3, loaded four blocks ahead
@@ -405,7 +401,7 @@ bool make_map(const System& s, void* base, CUtensorMap* map)
 
 }  // namespace
 
-bool make_pair_map(const System& s, bool fp32_terms, CUtensorMap* map, CUtensorMap* mapT)
+bool make_pair_map(const System& s, bool fp32_terms, CUtensorMap* map)
 {
     if (!fp32_terms)
         return make_map<double>(s, s.pairbuf, map) &&
@@ -413,22 +409,20 @@ bool make_pair_map(const System& s, bool fp32_terms, CUtensorMap* map, CUtensorM
                                     RsStage<1>::kSmem) == cudaSuccess &&
                cudaFuncSetAttribute(rowsum_tma_kernel<double, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     RsStage<2>::kSmem) == cudaSuccess;
-    return make_map<float>(s, s.pairbuf, map) && make_map<float>(s, s.pairT, mapT) &&
-           cudaFuncSetAttribute(rowsum_mixed_kernel<kRsStages>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    // the mixed form's tiles are contiguous: plain bulk copies, no tensor map
+    return cudaFuncSetAttribute(rowsum_mixed_kernel<kRsStages>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 MixShape<kRsStages>::kSmem) == cudaSuccess &&
            cudaFuncSetAttribute(rowsum_mixed_kernel<kMixDeepStages>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 MixShape<kMixDeepStages>::kSmem) == cudaSuccess;
 }
 
-void launch_rowsum_mixed(const System& s, const CUtensorMap& mapA, const CUtensorMap& mapT, int num_sms,
-                         cudaStream_t st)
+void launch_rowsum_mixed(const System& s, int num_sms, cudaStream_t st)
 {
     const int ctas = (3 * s.nb + kRsWarps - 1) / kRsWarps;
     if (ctas <= 3 * num_sms)  // every warp fits at 3 deep CTAs per SM
-        rowsum_mixed_kernel<kMixDeepStages><<<ctas, 32 * kRsWarps, MixShape<kMixDeepStages>::kSmem, st>>>(s, mapA,
-                                                                                                          mapT);
+        rowsum_mixed_kernel<kMixDeepStages><<<ctas, 32 * kRsWarps, MixShape<kMixDeepStages>::kSmem, st>>>(s);
     else
-        rowsum_mixed_kernel<kRsStages><<<ctas, 32 * kRsWarps, MixShape<kRsStages>::kSmem, st>>>(s, mapA, mapT);
+        rowsum_mixed_kernel<kRsStages><<<ctas, 32 * kRsWarps, MixShape<kRsStages>::kSmem, st>>>(s);
 }
 
 template <typename T>

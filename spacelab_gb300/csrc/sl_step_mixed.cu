@@ -45,10 +45,11 @@ __device__ __forceinline__ double fp64_d2(const System& s, int A, int B)
 
 // Same tiling as pair_tile_kernel: one warp per lower-triangular 32x32 block
 // tile, lane b = sphere 32Y+b, loop over the A block; terms stored as FP32:
-// sphere A's in the A-side buffer pA[c][A][B] (the float view of pairbuf),
-// sphere B's in the B-side buffer pairT[c][A][B] -- both indexed by (A, B),
-// so that both stores of a warp are coalesced over B.  Torques (contacts
-// only) go to the float view of torqbuf, [A][B] and [B][A].
+// sphere A's in the A-side buffer (the float view of pairbuf), sphere B's in
+// the B-side buffer pairT, both at mixed_term_index(A, B): tile (X, Y) of
+// both is 4 KB of contiguous memory and each of a warp's stores covers one
+// 128-byte row of it.  Torques (contacts only) go to the float view of
+// torqbuf, [A][B] and [B][A].
 template <bool WRITE>
 __global__ void __launch_bounds__(128, 4) mixed_pair_kernel(const __grid_constant__ System s)
 {
@@ -84,8 +85,11 @@ __global__ void __launch_bounds__(128, 4) mixed_pair_kernel(const __grid_constan
         const int a_end = min(kBlock, s.n - X * kBlock);
         double pe = 0;
         uint32_t rowbits = 0, colbits = 0;
-        float* rowA = pbuf + (size_t)(X * kBlock) * s.npad + B;      // + a npad: A-side term of row A
-        float* rowAT = s.pairT + (size_t)(X * kBlock) * s.npad + B;  // + a npad: B-side term, coalesced
+        // tile (X, Y) of both term buffers; element (a, lane) of row a is at
+        // a * 32 + swizzled lane, so a warp's store covers one 128-byte row
+        const size_t tile = ((size_t)X * s.nb + Y) * 1024;
+        float* tileA = pbuf + tile;
+        float* tileT = s.pairT + tile;
         for (int a = 0; a < a_end; ++a) {
             const bool valid = bvalid && (X != Y || lane < a);
             bool contact = false;
@@ -136,9 +140,10 @@ __global__ void __launch_bounds__(128, 4) mixed_pair_kernel(const __grid_constan
                     }
                 }
                 const float ima = ab.inv_m[a];
-                float* pa = rowA + (size_t)a * s.npad;
+                const int e = a * 32 + ((((lane >> 2) ^ (a & 7)) << 2) | (lane & 3));  // mixed_term_index
+                float* pa = tileA + e;
                 __stcs(pa, fx * ima); __stcs(pa + plane, fy * ima); __stcs(pa + 2 * plane, fz * ima);
-                float* pb = rowAT + (size_t)a * s.npad;
+                float* pb = tileT + e;
                 __stcs(pb, -fx * inv_mb); __stcs(pb + plane, -fy * inv_mb); __stcs(pb + 2 * plane, -fz * inv_mb);
             }
             const uint32_t bal = __ballot_sync(0xffffffffu, contact);
@@ -172,12 +177,12 @@ __global__ void __launch_bounds__(kMixThreads) mixed_rowsum_kernel(const __grid_
     const int i = t - c * s.n;
     const int n = s.n;
     const size_t plane = (size_t)s.npad * s.npad;
-    // partners j < i from the A-side row i, j > i from the B-side column i
-    const float* rowA = reinterpret_cast<const float*>(s.pairbuf) + c * plane + (size_t)i * s.npad;
-    const float* colT = s.pairT + c * plane + i;
+    // partners j < i from the A side (i, j), j > i from the B side (j, i)
+    const float* pA = reinterpret_cast<const float*>(s.pairbuf) + c * plane;
+    const float* pT = s.pairT + c * plane;
     double acc = 0.0;
-    for (int j = 0; j < i; ++j) acc += f2d_bits(__ldcs(rowA + j));
-    for (int j = i + 1; j < n; ++j) acc += f2d_bits(__ldcs(colT + (size_t)j * s.npad));
+    for (int j = 0; j < i; ++j) acc += f2d_bits(__ldcs(pA + mixed_term_index(s.nb, i, j)));
+    for (int j = i + 1; j < n; ++j) acc += f2d_bits(__ldcs(pT + mixed_term_index(s.nb, j, i)));
     double aacc = 0.0;
     const uint32_t* mrow = s.cmask + (size_t)i * s.nb;
     const float* trow = reinterpret_cast<const float*>(s.torqbuf) + c * plane + (size_t)i * s.npad;
@@ -201,8 +206,7 @@ __global__ void __launch_bounds__(kMixThreads) mixed_rowsum_kernel(const __grid_
 
 }  // namespace
 
-void launch_step_mixed(const System& s, bool write, int num_sms, cudaStream_t st, StepTimers* tm,
-                       const CUtensorMap* map, const CUtensorMap* mapT)
+void launch_step_mixed(const System& s, bool write, int num_sms, cudaStream_t st, StepTimers* tm, bool bulk_rows)
 {
     launch_drift(s, st);
     if (tm) cudaEventRecord(tm->ev[0], st);
@@ -214,8 +218,8 @@ void launch_step_mixed(const System& s, bool write, int num_sms, cudaStream_t st
     else
         mixed_pair_kernel<false><<<pb, 128, 0, st>>>(s);
     if (tm) cudaEventRecord(tm->ev[1], st);
-    if (map && mapT)
-        launch_rowsum_mixed(s, *map, *mapT, num_sms, st);
+    if (bulk_rows)
+        launch_rowsum_mixed(s, num_sms, st);
     else
         mixed_rowsum_kernel<<<(3 * s.n + kMixThreads - 1) / kMixThreads, kMixThreads, 0, st>>>(s);
     if (tm) cudaEventRecord(tm->ev[2], st);

@@ -78,5 +78,14 @@ __device__ __forceinline__ void load_2d(void* dst, const CUtensorMap* map, int x
         : "memory");
 }
 
+// 1D bulk copy of `bytes` (a multiple of 16) from global `src` into dst;
+// both 16-byte aligned; completes `bar`'s transaction count.
+__device__ __forceinline__ void load_1d(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(smem_addr(dst)), "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+
 }  // namespace tma
 }  // namespace sl
