@@ -245,11 +245,12 @@ __device__ __forceinline__ void rs_cols(const unsigned char* stage, int lane, fl
         v[a] = *reinterpret_cast<const float*>(stage + a * 128 + ((((lane >> 2) ^ (a & 7)) << 4) | ((lane & 3) << 2)));
 }
 
-// NST stages of one box per warp: kRsStages when the system's warps are many
-// (16 warps share an SM), kMixDeepStages when they are few -- a stage holds
-// only ~150 cycles of adds here, so many copies must be in flight to cover
-// the TMA latency.
-constexpr int kMixDeepStages = 8;
+// NST stages of one box per warp.  SPLIT = 1: the CTA's kRsWarps warps own
+// one row block each.  SPLIT = 2 (systems whose warps are few): the two warps
+// of a CTA share one row block, each summing half of its partner tiles, and
+// warp 0 adds warp 1's sums -- twice the copies in flight per row, which the
+// bandwidth of these tile reads needs.
+constexpr int kMixDeepStages = 6;
 
 template <int NST>
 struct MixShape {
@@ -257,18 +258,20 @@ struct MixShape {
     static constexpr int kSmem = kRsWarps * kWarpBytes + 1024;  // + alignment slack
 };
 
-template <int NST>
-__global__ void __launch_bounds__(32 * kRsWarps, NST == kRsStages ? 8 : 3)
+template <int NST, int SPLIT>
+__global__ void __launch_bounds__(32 * kRsWarps, NST == kRsStages ? 8 : 4)
     rowsum_mixed_kernel(const __grid_constant__ System s)
 {
     constexpr int kRsStages = NST;  // shadows the file-wide depth in this kernel
     using Stage = MixShape<NST>;
     extern __shared__ unsigned char rs_raw[];
     __shared__ __align__(8) uint64_t full_all[kRsWarps][kRsStages];
+    __shared__ double part[2][kBlock];  // SPLIT = 2: warp 1's force and torque sums
+    __shared__ int part_bad;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
-    const int wg = blockIdx.x * kRsWarps + warp;
-    if (wg >= 3 * s.nb) return;  // no block-wide synchronisation below
+    const int wg = SPLIT == 1 ? blockIdx.x * kRsWarps + warp : blockIdx.x;  // (component, row block)
+    if (SPLIT == 1 && wg >= 3 * s.nb) return;  // no block-wide synchronisation when SPLIT == 1
     unsigned char* buf = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(rs_raw) + 1023) &
                                                           ~static_cast<uintptr_t>(1023)) +
                          warp * Stage::kWarpBytes;
@@ -276,14 +279,18 @@ __global__ void __launch_bounds__(32 * kRsWarps, NST == kRsStages ? 8 : 3)
     const int c = wg / s.nb;
     const int rb = wg - c * s.nb;
     const int i = rb * kBlock + lane;  // < npad
-    const int nq = s.nb + 1;
+    // this warp's stages q0 .. q1-1 of the row block's nb + 1
+    const int half = (s.nb + 1) / 2;
+    const int q0 = SPLIT == 2 && warp == 1 ? half : 0;
+    const int q1 = SPLIT == 2 && warp == 0 ? half : s.nb + 1;
+    const int nq = q1 - q0;
     const size_t plane = (size_t)s.npad * s.npad;
     const float* pA = reinterpret_cast<const float*>(s.pairbuf) + c * plane;
     const float* pT = s.pairT + c * plane;
     // stage q: A-side tile (I, q) for q <= I, B-side tile (q - 1, I) after;
     // each is 4 KB of contiguous memory (mixed_term_index), one bulk copy
-    auto issue = [&](int q) {
-        const int st = q % kRsStages;
+    auto issue = [&](int k) {  // k-th stage of this warp
+        const int q = q0 + k, st = k % kRsStages;
         const float* src = q <= rb ? pA + ((size_t)rb * s.nb + q) * 1024 : pT + ((size_t)(q - 1) * s.nb + rb) * 1024;
         tma::mbar_arrive_expect_tx(&full[st], kRsBox);
         tma::load_1d(buf + st * kRsBox, src, kRsBox, &full[st]);
@@ -291,7 +298,7 @@ __global__ void __launch_bounds__(32 * kRsWarps, NST == kRsStages ? 8 : 3)
     if (lane == 0) {
         for (int k = 0; k < kRsStages; ++k) tma::mbar_init(&full[k], 1);
         tma::fence_barrier_init();
-        for (int q = 0; q < nq && q < kRsStages; ++q) issue(q);
+        for (int k = 0; k < nq && k < kRsStages; ++k) issue(k);
     }
     __syncwarp();
 
@@ -302,42 +309,51 @@ __global__ void __launch_bounds__(32 * kRsWarps, NST == kRsStages ? 8 : 3)
     df::Sum acc[kLanes] = {}, aacc{0.0f, 0.0f};
     const uint32_t* mrow = s.cmask + (size_t)i * s.nb;  // rows < npad exist; padding rows are 0
     const float* trow = reinterpret_cast<const float*>(s.torqbuf) + c * plane + (size_t)i * s.npad;
-    // contact-mask words of partner blocks J .. J+3, loaded four blocks ahead
-    // (a stage's adds take too few cycles to cover a global load)
-    uint32_t w0 = mrow[0], w1 = s.nb > 1 ? mrow[1] : 0u, w2 = s.nb > 2 ? mrow[2] : 0u, w3 = s.nb > 3 ? mrow[3] : 0u;
+    // partner block of stage q (the diagonal's A part, q == rb, has none of
+    // its own: its torque terms follow the B part); contact-mask words of the
+    // next four partner blocks are loaded ahead, a stage's adds taking too
+    // few cycles to cover a global load
+    auto block_of = [&](int q) { return q < rb ? q : q - 1; };
+    const int J0 = block_of(q0 == rb ? q0 + 1 : q0);
+    auto mask = [&](int J) { return J < s.nb && J <= block_of(q1 - 1) ? mrow[J] : 0u; };
+    uint32_t w0 = mask(J0), w1 = mask(J0 + 1), w2 = mask(J0 + 2), w3 = mask(J0 + 3);
     float cur[kBlock], nxt[kBlock];
-    int waited = 0;  // first stage not yet observed complete
-    bool ok = __all_sync(0xffffffffu, tma::mbar_wait(&full[0], 0));
-    if (ok) {
-        rs_rows(buf, lane, cur);  // stage 0 is always A-side rows
+    int waited = 0;  // first of this warp's stages not yet observed complete
+    bool ok = nq <= 0 || __all_sync(0xffffffffu, tma::mbar_wait(&full[0], 0));
+    if (ok && nq > 0) {
+        if (q0 <= rb)
+            rs_rows(buf, lane, cur);
+        else
+            rs_cols(buf, lane, cur);
         waited = 1;
     }
-    for (int q = 0; ok && q < nq; ++q) {
-        __syncwarp();  // every lane has stage q in registers: its buffer is free
-        if (lane == 0 && q + kRsStages < nq) {
+    for (int k = 0; ok && k < nq; ++k) {
+        const int q = q0 + k;
+        __syncwarp();  // every lane has stage k in registers: its buffer is free
+        if (lane == 0 && k + kRsStages < nq) {
             tma::fence_proxy_async();
-            issue(q + kRsStages);
+            issue(k + kRsStages);
         }
-        if (q + 1 < nq) {
-            const int st1 = (q + 1) % kRsStages;
-            ok = __all_sync(0xffffffffu, tma::mbar_wait(&full[st1], ((q + 1) / kRsStages) & 1));
+        if (k + 1 < nq) {
+            const int st1 = (k + 1) % kRsStages;
+            ok = __all_sync(0xffffffffu, tma::mbar_wait(&full[st1], ((k + 1) / kRsStages) & 1));
             if (ok) {
                 if (q + 1 <= rb)
                     rs_rows(buf + st1 * kRsBox, lane, nxt);
                 else
                     rs_cols(buf + st1 * kRsBox, lane, nxt);
-                waited = q + 2;
+                waited = k + 2;
             }
         }
 #pragma unroll
         for (int a = 0; a < kBlock; ++a) acc[a % kLanes].add(cur[a]);
         if (q != rb) {  // partner block J complete (the diagonal after its B part): torque terms
-            const int J = q < rb ? q : q - 1;
+            const int J = block_of(q);
             uint32_t wd = w0;
             w0 = w1;
             w1 = w2;
             w2 = w3;
-            w3 = J + 4 < s.nb ? mrow[J + 4] : 0u;
+            w3 = mask(J + 4);
             while (wd) {
                 const int bit = __ffs(wd) - 1;
                 wd &= wd - 1;
@@ -349,15 +365,26 @@ __global__ void __launch_bounds__(32 * kRsWarps, NST == kRsStages ? 8 : 3)
     }
     if (!ok) {
         const int issued = min(nq, waited + kRsStages);
-        for (int qq = waited; qq < issued; ++qq) tma::mbar_wait(&full[qq % kRsStages], (qq / kRsStages) & 1);
+        for (int kk = waited; kk < issued; ++kk) tma::mbar_wait(&full[kk % kRsStages], (kk / kRsStages) & 1);
         if (lane == 0) atomicOr(s.status, kStatusWaitTimeoutBit);
-        return;
     }
-    if (i >= s.n) return;
     double fa = 0.0;
 #pragma unroll
     for (int k = 0; k < kLanes; ++k) fa += f2d_bits(acc[k].s) + f2d_bits(acc[k].c);
-    const double ta = f2d_bits(aacc.s) + f2d_bits(aacc.c);
+    double ta = f2d_bits(aacc.s) + f2d_bits(aacc.c);
+    if (SPLIT == 2) {  // both warps reach this barrier, failed or not
+        if (warp == 1) {
+            part[0][lane] = fa;
+            part[1][lane] = ta;
+            if (lane == 0) part_bad = ok ? 0 : 1;
+        }
+        __syncthreads();
+        if (warp == 1) return;
+        fa += part[0][lane];
+        ta += part[1][lane];
+        ok = ok && !part_bad;
+    }
+    if (!ok || i >= s.n) return;
     s.acc.c[c][i] = fa;
     s.aacc.c[c][i] = ta;
     const double dt = s.sc->dt;
@@ -410,19 +437,19 @@ bool make_pair_map(const System& s, bool fp32_terms, CUtensorMap* map)
                cudaFuncSetAttribute(rowsum_tma_kernel<double, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     RsStage<2>::kSmem) == cudaSuccess;
     // the mixed form's tiles are contiguous: plain bulk copies, no tensor map
-    return cudaFuncSetAttribute(rowsum_mixed_kernel<kRsStages>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    return cudaFuncSetAttribute(rowsum_mixed_kernel<kRsStages, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 MixShape<kRsStages>::kSmem) == cudaSuccess &&
-           cudaFuncSetAttribute(rowsum_mixed_kernel<kMixDeepStages>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+           cudaFuncSetAttribute(rowsum_mixed_kernel<kMixDeepStages, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 MixShape<kMixDeepStages>::kSmem) == cudaSuccess;
 }
 
 void launch_rowsum_mixed(const System& s, int num_sms, cudaStream_t st)
 {
-    const int ctas = (3 * s.nb + kRsWarps - 1) / kRsWarps;
-    if (ctas <= 3 * num_sms)  // every warp fits at 3 deep CTAs per SM
-        rowsum_mixed_kernel<kMixDeepStages><<<ctas, 32 * kRsWarps, MixShape<kMixDeepStages>::kSmem, st>>>(s);
+    if (3 * s.nb <= 4 * num_sms)  // every row block's CTA fits at 4 deep CTAs per SM: two warps per row block
+        rowsum_mixed_kernel<kMixDeepStages, 2><<<3 * s.nb, 32 * kRsWarps, MixShape<kMixDeepStages>::kSmem, st>>>(s);
     else
-        rowsum_mixed_kernel<kRsStages><<<ctas, 32 * kRsWarps, MixShape<kRsStages>::kSmem, st>>>(s);
+        rowsum_mixed_kernel<kRsStages, 1><<<(3 * s.nb + kRsWarps - 1) / kRsWarps, 32 * kRsWarps,
+                                            MixShape<kRsStages>::kSmem, st>>>(s);
 }
 
 template <typename T>
