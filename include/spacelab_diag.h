@@ -39,6 +39,9 @@ int sl_diag_fp64_add_latency(int warps_per_sm, int active_lanes, double* cycles_
  * with CUDA events. */
 int sl_diag_fp64_peak(double* gflops);
 
+/* The same for FP32 fused multiply-adds (the mixed form's pipe). */
+int sl_diag_fp32_peak(double* gflops);
+
 #ifdef __cplusplus
 }
 #endif

@@ -105,6 +105,7 @@ _PROTOS = [
     # diagnostics (spacelab_diag.h)
     ("sl_diag_division", ctypes.c_int, [ctypes.c_int] + [_c_double_p] * 4),
     ("sl_diag_fp64_peak", ctypes.c_int, [_c_double_p]),
+    ("sl_diag_fp32_peak", ctypes.c_int, [_c_double_p]),
     ("sl_diag_fp64_add_latency", ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     ("sl_diag_exact_ops", ctypes.c_int, [ctypes.c_int] + [_c_double_p] * 3),
 ("sl_diag_int_ops", ctypes.c_int, [ctypes.c_int] + [_c_double_p] * 3),

@@ -62,7 +62,7 @@ struct sl_handle {
     // exact mode: side stream + events overlapping row sums with pair phases
     sl::StepOverlap ov{};
     CUtensorMap pair_map{};  // exact form: the pair-term buffer for the TMA row sums
-    bool has_map = false;     // the bulk-copy row sums are ready
+    bool has_map = false;     // the TMA row sums are ready (exact form)
     bool has_ov = false;   // ov's stream and events exist
     bool overlap = false;  // steps use them
     void* arena = nullptr;
@@ -95,7 +95,7 @@ int check_handle(const sl_handle* h)
 void launch_mode_step(sl_handle* h, bool write, sl::StepTimers* tm)
 {
     if (h->mode == SL_MODE_MIXED)
-        sl::launch_step_mixed(h->sys, write, h->num_sms, h->stream, tm, h->has_map);
+        sl::launch_step_mixed(h->sys, write, h->num_sms, h->stream, tm);
     else
         sl::launch_step(h->sys, write, h->num_sms, h->stream, tm, h->overlap ? &h->ov : nullptr,
                         h->has_map ? &h->pair_map : nullptr);
@@ -218,8 +218,11 @@ int sl_create(int n, const sl_material* mat, int mode, sl_handle** out)
     size_t o_f[10] = {};
     if (mode == SL_MODE_MIXED)
         for (int k = 0; k < 10; ++k) o_f[k] = take(np * sizeof(float));
-    const size_t o_pair = take(3 * np * np * sizeof(double));
-    const size_t o_torq = take(3 * np * np * sizeof(double));
+    // the mixed form keeps per-tile partial sums instead of pair terms, and
+    // FP32 torque terms
+    const bool mixed = mode == SL_MODE_MIXED;
+    const size_t o_pair = take(mixed ? 3 * (size_t)s.nb * np * sizeof(float) : 3 * np * np * sizeof(double));
+    const size_t o_torq = take(3 * np * np * (mixed ? sizeof(float) : sizeof(double)));
     const size_t o_mask = take(np * s.nb * sizeof(uint32_t));
     const size_t o_pe = take((size_t)s.ntiles * sizeof(double));
     const size_t o_red = take(sl::kRedBlocks * 8 * sizeof(double));
@@ -245,8 +248,10 @@ int sl_create(int n, const sl_material* mat, int mode, sl_handle** out)
         s.f_Rlo = reinterpret_cast<float*>(base + o_f[3]);
         for (int k = 0; k < 6; ++k) s.f_pos[k] = reinterpret_cast<float*>(base + o_f[4 + k]);
     }
-    s.pairbuf = reinterpret_cast<double*>(base + o_pair);
-    if (mode == SL_MODE_MIXED) s.pairT = reinterpret_cast<float*>(s.pairbuf) + 3 * np * np;
+    if (mixed)
+        s.f_part = reinterpret_cast<float*>(base + o_pair);
+    else
+        s.pairbuf = reinterpret_cast<double*>(base + o_pair);
     s.torqbuf = reinterpret_cast<double*>(base + o_torq);
     s.cmask = reinterpret_cast<uint32_t*>(base + o_mask);
     s.pe_tile = reinterpret_cast<double*>(base + o_pe);
@@ -256,7 +261,7 @@ int sl_create(int n, const sl_material* mat, int mode, sl_handle** out)
     h->d_sc = reinterpret_cast<sl::Scalars*>(base + o_scl);
     h->d_stage = reinterpret_cast<double*>(base + o_dstage);
     s.sc = h->d_sc;
-    h->has_map = sl::make_pair_map(s, mode == SL_MODE_MIXED, &h->pair_map);
+    h->has_map = !mixed && sl::make_pair_map(s, &h->pair_map);
     e = cudaMemsetAsync(h->arena, 0, h->arena_bytes, h->stream);
     if (e != cudaSuccess) { sl_destroy(h); return cuda_fail(e, "cudaMemset"); }
     e = cudaMallocHost(&h->staging, 18 * np * sizeof(double));
@@ -480,7 +485,8 @@ int sl_contacts(sl_handle* h, int* pairs, long max_pairs, long* count)
     long c = 0;
     for (int A = 0; A < s.n; ++A) {
         for (int Y = 0; Y <= A / sl::kBlock; ++Y) {
-            uint32_t wd = mask[(size_t)A * s.nb + Y];
+            // [npad][nb] in the exact form, [nb][npad] in the mixed form
+            uint32_t wd = h->mode == SL_MODE_MIXED ? mask[(size_t)Y * s.npad + A] : mask[(size_t)A * s.nb + Y];
             while (wd) {
                 const int b = __builtin_ctz(wd);
                 wd &= wd - 1;

@@ -14,7 +14,11 @@
 //                                            s adds to acc[s] (scratch)
 //   torqbuf[3][npad][npad]                   per-pair torque contributions,
 //                                            written only for contacts
-//   cmask[npad][nb]                          contact bit per (s, 32-block)
+//   cmask[npad][nb]                          contact bit per (s, 32-block);
+//                                            the mixed form stores it
+//                                            [nb][npad] (block-major)
+//   f_part[3][nb][npad]                      mixed form only: per-tile
+//                                            partial sums (pairbuf unused)
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -60,24 +64,12 @@ struct System {
     // of the scaled positions (x, y, z hi, then x, y, z lo), the latter
     // written by the drift kernel every step
     float *f_Rlo, *f_pos[6];
-    // the mixed form's B-side pair terms (FP32): sphere B's term from partner
-    // A, at mixed_term_index(A, B); it is the upper half of pairbuf, whose
-    // FP32 view the A-side terms fill only in part
-    float* pairT;
+    // the mixed form's per-tile partial sums [3][nb][npad] (FP32): entry
+    // (c, K, i) is component c of sphere i's acceleration terms from the
+    // partners in 32-sphere block K
+    float* f_part;
     int len_shift;
 };
-
-// The mixed form's pair-term layout (A side in the FP32 view of pairbuf, B
-// side in pairT, each [3] planes of npad^2 floats): tile-major, 32 x 32
-// tiles of 4 KB stored contiguously, tile (I, J) at (I nb + J) * 1024, and
-// inside a tile row a's 16-byte chunks permuted by XOR with (a & 7) -- the
-// 128-byte swizzle -- so that a tile copied to shared memory as one block
-// can be read by rows or by columns without bank conflicts.
-__device__ __forceinline__ size_t mixed_term_index(int nb, int A, int B)
-{
-    const int a = A & 31, b = B & 31;
-    return ((size_t)(A >> 5) * nb + (B >> 5)) * 1024 + a * 32 + ((((b >> 2) ^ (a & 7)) << 2) | (b & 3));
-}
 
 // Operands of a pair's contact branch beyond positions and radii (the
 // contact branch is rare: O(N) of the O(N^2) pairs, so they are gathered
@@ -158,7 +150,9 @@ __device__ __forceinline__ double div_by_recip(double a, double b, double y)
 // Lower-triangular tile index t -> (X, Y), X >= Y, t = X(X+1)/2 + Y.
 __device__ __forceinline__ void tile_coords(long long t, int& X, int& Y)
 {
-    long long x = (long long)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+    // FP32 estimate (the FP64 pipe is slow), corrected exactly below
+    long long x = (long long)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
+    if (x < 0) x = 0;
     while (x * (x + 1) / 2 > t) --x;
     while ((x + 1) * (x + 2) / 2 <= t) ++x;
     X = (int)x;

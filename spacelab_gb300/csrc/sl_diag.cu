@@ -101,6 +101,50 @@ __global__ void fma_chain_kernel(double* out, double seed)
     out[t] = s;
 }
 
+constexpr int kIters32 = 16384;
+
+__global__ void fma32_chain_kernel(float* out, float seed)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    float v[kChains];
+#pragma unroll
+    for (int k = 0; k < kChains; ++k) v[k] = seed + t * 1e-6f + k;
+    const float b = 0.9999f, c = 1e-4f;
+    for (int i = 0; i < kIters32; ++i) {
+#pragma unroll
+        for (int k = 0; k < kChains; ++k) v[k] = fmaf(v[k], b, c);
+    }
+    float s = 0;
+#pragma unroll
+    for (int k = 0; k < kChains; ++k) s += v[k];
+    out[t] = s;
+}
+
+// Best-of-3 time (after one untimed launch) of `launch`, in ms; <0 on error.
+template <typename F>
+float best_time_ms(F launch)
+{
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    for (int rep = 0; rep < 4; ++rep) {
+        cudaEventRecord(e0);
+        launch();
+        cudaEventRecord(e1);
+        if (cudaEventSynchronize(e1) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
+            best = -1.0f;
+            break;
+        }
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0 && ms < best) best = ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return best;
+}
+
 }  // namespace
 
 extern "C" int sl_diag_division(int n, const double* a, const double* b, double* q_recip, double* q_ieee)
@@ -176,25 +220,28 @@ extern "C" int sl_diag_fp64_peak(double* gflops)
     const int blocks = sms * 8, threads = 256;
     double* out = nullptr;
     if (cudaMalloc(&out, (size_t)blocks * threads * sizeof(double)) != cudaSuccess) return SL_ERR_ALLOC;
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
-    float best = 1e30f;
-    int rc = SL_OK;
-    for (int rep = 0; rep < 4 && rc == SL_OK; ++rep) {
-        cudaEventRecord(e0);
-        fma_chain_kernel<<<blocks, threads>>>(out, 1.0);
-        cudaEventRecord(e1);
-        if (cudaEventSynchronize(e1) != cudaSuccess || cudaGetLastError() != cudaSuccess) rc = SL_ERR_CUDA;
-        float ms = 0;
-        cudaEventElapsedTime(&ms, e0, e1);
-        if (rep > 0 && ms < best) best = ms;
-    }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    const float best = best_time_ms([&] { fma_chain_kernel<<<blocks, threads>>>(out, 1.0); });
     cudaFree(out);
-    if (rc != SL_OK) return rc;
+    if (best <= 0) return SL_ERR_CUDA;
     const double flops = 2.0 * blocks * threads * (double)kChains * kIters;
+    *gflops = flops / (best * 1e-3) / 1e9;
+    return SL_OK;
+}
+
+extern "C" int sl_diag_fp32_peak(double* gflops)
+{
+    if (!gflops) return SL_ERR_ARG;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return SL_ERR_CUDA;
+    const int blocks = sms * 8, threads = 256;
+    float* out = nullptr;
+    if (cudaMalloc(&out, (size_t)blocks * threads * sizeof(float)) != cudaSuccess) return SL_ERR_ALLOC;
+    const float best = best_time_ms([&] { fma32_chain_kernel<<<blocks, threads>>>(out, 1.0f); });
+    cudaFree(out);
+    if (best <= 0) return SL_ERR_CUDA;
+    const double flops = 2.0 * blocks * threads * (double)kChains * kIters32;
     *gflops = flops / (best * 1e-3) / 1e9;
     return SL_OK;
 }

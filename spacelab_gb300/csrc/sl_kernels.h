@@ -37,23 +37,18 @@ void launch_stage_out(const System& s, double* stage, Vec3Soa* const arr[6], uns
 // TMA-streamed row sums; NULL the plain-load form.
 void launch_step(const System& s, bool write, int num_sms, cudaStream_t st, StepTimers* tm,
                  const StepOverlap* ov = nullptr, const CUtensorMap* map = nullptr);
-// Prepares the bulk-copy row sums: the exact form's tensor map of the
-// pair-term buffer (FP64), or, for the mixed form (fp32_terms), only the
-// kernels' shared-memory limits; false if that fails (the plain-load row
-// sums are used then).
-bool make_pair_map(const System& s, bool fp32_terms, CUtensorMap* map);
-// The mixed form's bulk-copy row sums (A-side rows and B-side columns).
-void launch_rowsum_mixed(const System& s, int num_sms, cudaStream_t st);
+// Prepares the TMA row sums of the exact form: the tensor map of the
+// pair-term buffer (FP64) and the kernels' shared-memory limits; false if
+// that fails (the plain-load row sums are used then).
+bool make_pair_map(const System& s, CUtensorMap* map);
 // The TMA-streamed ordered row sums over partner blocks [b0, b1) with terms
-// of type T (double: exact form, float: mixed form); first/last as for the
-// plain row sums.
+// of type T (double); first/last as for the plain row sums.
 template <typename T>
 void launch_rowsum_tma(const System& s, const CUtensorMap& map, int b0, int b1, int first, int last, int num_sms,
                        cudaStream_t st);
 // Status bit set by a kernel whose bounded wait for a TMA copy ran out.
 constexpr unsigned kStatusWaitTimeoutBit = 2u;
-void launch_step_mixed(const System& s, bool write, int num_sms, cudaStream_t st, StepTimers* tm,
-                       bool bulk_rows = false);
+void launch_step_mixed(const System& s, bool write, int num_sms, cudaStream_t st, StepTimers* tm);
 void launch_drift(const System& s, cudaStream_t st);
 void launch_energy(const System& s, cudaStream_t st);
 int pair_grid_blocks(long long tiles, int num_sms);

@@ -21,6 +21,34 @@ __device__ __forceinline__ float vdw_shape(float h, float Ra, float Rb)
     return __fdividef(r3 * (h + sum), (S * S) * (T * T));
 }
 
+// The vdW potential's bracket 2RaRb/P + 2RaRb/Q + ln(P/Q), P = z^2 - (Ra+Rb)^2,
+// Q = z^2 - (Ra-Rb)^2 (ColliderSingleCore.cpp:228-240; U = -Ha/6 times it),
+// for a pair at centre distance z >= 2 (Ra + Rb), from d2 = z^2 in scaled
+// lengths.  With u = 4 Ra Rb / Q (P/Q = 1 - u) the bracket is
+// u/(2(1-u)) + u/2 + ln(1-u) = sum_{k>=3} (k-2)/(2k) u^k: its O(u) and
+// O(u^2) parts cancel exactly, which the closed form resolves only in FP64.
+// Here u <= 1/4, so the terms up to k = 15 leave a relative truncation
+// error below 5e-8, and FP32 Horner evaluation suffices.
+__device__ __forceinline__ float vdw_bracket_far(float d2, float Ra, float Rb)
+{
+    const float dd = Ra - Rb;
+    const float u = __fdividef(4.0f * Ra * Rb, fmaf(-dd, dd, d2));
+    float p = 13.0f / 30.0f;                 // k = 15
+    p = fmaf(p, u, 3.0f / 7.0f);             // 14
+    p = fmaf(p, u, 11.0f / 26.0f);           // 13
+    p = fmaf(p, u, 5.0f / 12.0f);            // 12
+    p = fmaf(p, u, 9.0f / 22.0f);            // 11
+    p = fmaf(p, u, 2.0f / 5.0f);             // 10
+    p = fmaf(p, u, 7.0f / 18.0f);            // 9
+    p = fmaf(p, u, 3.0f / 8.0f);             // 8
+    p = fmaf(p, u, 5.0f / 14.0f);            // 7
+    p = fmaf(p, u, 1.0f / 3.0f);             // 6
+    p = fmaf(p, u, 3.0f / 10.0f);            // 5
+    p = fmaf(p, u, 1.0f / 4.0f);             // 4
+    p = fmaf(p, u, 1.0f / 6.0f);             // 3
+    return (u * u) * (u * p);
+}
+
 struct ContactF {
     float fx, fy, fz, tax, tay, taz, tbx, tby, tbz;
     double k;  // spring constant chosen for this step (for the write-step PE)

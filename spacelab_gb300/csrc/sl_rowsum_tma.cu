@@ -1,16 +1,14 @@
 // sl_rowsum_tma.cu -- the ordered row sums (pass 2's accumulation, then
 // pass 3) with the pair terms streamed into shared memory by the bulk-copy
 // (TMA) engine: rowsum_tma_kernel for the exact form's FP64 terms (tensor-
-// map boxes of row-major rows), rowsum_mixed_kernel for the mixed form's
-// FP32 terms (whole tiles, A-side rows and B-side columns, see there).
+// map boxes of row-major rows).
 //
 // Thread (c, i) adds acc_c[i] = sum over partners j ascending of
 // pairbuf[c][i][j] -- the order in which the reference adds terms to acc[i]
 // and aacc[i] (ColliderSingleCore.cpp:100-103, 249-250) -- over the partner
 // blocks [b0, b1), continuing the running sums kept in acc/aacc between
 // segments; the last segment does pass 3 (:263-267).  FP64 terms are added
-// in FP64 (the reference's own additions); the mixed form's FP32 terms are
-// added in a compensated double-float sum on the FP32 pipe (sl_df.cuh).
+// in FP64 (the reference's own additions).
 //
 // Layout: one warp per (component, 32-row block), lane = row, kRsWarps
 // independent warps per CTA so that the warps and their FP64 add chains
@@ -35,7 +33,6 @@
 // unit bounds.
 #include "sl_device.cuh"
 #include "sl_kernels.h"
-#include "sl_df.cuh"
 #include "sl_tma.cuh"
 
 #include <cudaTypedefs.h>
@@ -213,188 +210,6 @@ __global__ void __launch_bounds__(32 * kRsWarps, 8 / BPS) rowsum_tma_kernel(cons
     if (!isfinite(v) || !isfinite(wv) || !isfinite(s.pos.c[c][i])) atomicOr(s.status, 1u);
 }
 
-// ---------------------------------------------------------------------------
-// Mixed form.  Row i's FP32 terms for partners j < i (i is the A sphere) are
-// the A-side entries (i, j); for j > i (i is B) the B-side entries (j, i),
-// both in the tile-major swizzled layout of mixed_term_index, so that one
-// bulk copy brings a whole 32 x 32 tile.  Stage q of row block I is A-side
-// tile (I, q) read by rows for q <= I (on the diagonal tile the entries
-// j >= i are never written and hold +0.0), and B-side tile (q-1, I) read by
-// columns for q > I (on the diagonal the entries j <= i hold +0.0).  Every entry of
-// every stage is added, in ascending j, into four interleaved compensated
-// sums (the mixed form is not bound to the reference's rounding sequence;
-// the sums are near exact either way).
-__device__ __forceinline__ void rs_rows(const unsigned char* stage, int lane, float (&v)[kBlock])
-{
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        const uint4 u = rs_chunk(stage, lane, k);
-        v[4 * k] = __uint_as_float(u.x);
-        v[4 * k + 1] = __uint_as_float(u.y);
-        v[4 * k + 2] = __uint_as_float(u.z);
-        v[4 * k + 3] = __uint_as_float(u.w);
-    }
-}
-
-// column `lane` of a swizzled 32 x 32 float box: at each row the lanes' 4-byte
-// reads cover the row's 128 bytes once (no bank conflict)
-__device__ __forceinline__ void rs_cols(const unsigned char* stage, int lane, float (&v)[kBlock])
-{
-#pragma unroll
-    for (int a = 0; a < kBlock; ++a)
-        v[a] = *reinterpret_cast<const float*>(stage + a * 128 + ((((lane >> 2) ^ (a & 7)) << 4) | ((lane & 3) << 2)));
-}
-
-// NST stages of one box per warp.  SPLIT = 1: the CTA's kRsWarps warps own
-// one row block each.  SPLIT = 2 (systems whose warps are few): the two warps
-// of a CTA share one row block, each summing half of its partner tiles, and
-// warp 0 adds warp 1's sums -- twice the copies in flight per row, which the
-// bandwidth of these tile reads needs.
-constexpr int kMixDeepStages = 6;
-
-template <int NST>
-struct MixShape {
-    static constexpr int kWarpBytes = NST * kRsBox;
-    static constexpr int kSmem = kRsWarps * kWarpBytes + 1024;  // + alignment slack
-};
-
-template <int NST, int SPLIT>
-__global__ void __launch_bounds__(32 * kRsWarps, NST == kRsStages ? 8 : 4)
-    rowsum_mixed_kernel(const __grid_constant__ System s)
-{
-    constexpr int kRsStages = NST;  // shadows the file-wide depth in this kernel
-    using Stage = MixShape<NST>;
-    extern __shared__ unsigned char rs_raw[];
-    __shared__ __align__(8) uint64_t full_all[kRsWarps][kRsStages];
-    __shared__ double part[2][kBlock];  // SPLIT = 2: warp 1's force and torque sums
-    __shared__ int part_bad;
-    const int lane = threadIdx.x & 31;
-    const int warp = threadIdx.x >> 5;
-    const int wg = SPLIT == 1 ? blockIdx.x * kRsWarps + warp : blockIdx.x;  // (component, row block)
-    if (SPLIT == 1 && wg >= 3 * s.nb) return;  // no block-wide synchronisation when SPLIT == 1
-    unsigned char* buf = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(rs_raw) + 1023) &
-                                                          ~static_cast<uintptr_t>(1023)) +
-                         warp * Stage::kWarpBytes;
-    uint64_t* full = full_all[warp];
-    const int c = wg / s.nb;
-    const int rb = wg - c * s.nb;
-    const int i = rb * kBlock + lane;  // < npad
-    // this warp's stages q0 .. q1-1 of the row block's nb + 1
-    const int half = (s.nb + 1) / 2;
-    const int q0 = SPLIT == 2 && warp == 1 ? half : 0;
-    const int q1 = SPLIT == 2 && warp == 0 ? half : s.nb + 1;
-    const int nq = q1 - q0;
-    const size_t plane = (size_t)s.npad * s.npad;
-    const float* pA = reinterpret_cast<const float*>(s.pairbuf) + c * plane;
-    const float* pT = s.pairT + c * plane;
-    // stage q: A-side tile (I, q) for q <= I, B-side tile (q - 1, I) after;
-    // each is 4 KB of contiguous memory (mixed_term_index), one bulk copy
-    auto issue = [&](int k) {  // k-th stage of this warp
-        const int q = q0 + k, st = k % kRsStages;
-        const float* src = q <= rb ? pA + ((size_t)rb * s.nb + q) * 1024 : pT + ((size_t)(q - 1) * s.nb + rb) * 1024;
-        tma::mbar_arrive_expect_tx(&full[st], kRsBox);
-        tma::load_1d(buf + st * kRsBox, src, kRsBox, &full[st]);
-    };
-    if (lane == 0) {
-        for (int k = 0; k < kRsStages; ++k) tma::mbar_init(&full[k], 1);
-        tma::fence_barrier_init();
-        for (int k = 0; k < nq && k < kRsStages; ++k) issue(k);
-    }
-    __syncwarp();
-
-    // four compensated sums (terms a = 0, 1, 2, 3 mod 4 of each block), so
-    // that a lane has four independent FP32 add chains in flight; their
-    // FP64 total is formed at the end
-    constexpr int kLanes = 4;
-    df::Sum acc[kLanes] = {}, aacc{0.0f, 0.0f};
-    const uint32_t* mrow = s.cmask + (size_t)i * s.nb;  // rows < npad exist; padding rows are 0
-    const float* trow = reinterpret_cast<const float*>(s.torqbuf) + c * plane + (size_t)i * s.npad;
-    // partner block of stage q (the diagonal's A part, q == rb, has none of
-    // its own: its torque terms follow the B part); contact-mask words of the
-    // next four partner blocks are loaded ahead, a stage's adds taking too
-    // few cycles to cover a global load
-    auto block_of = [&](int q) { return q < rb ? q : q - 1; };
-    const int J0 = block_of(q0 == rb ? q0 + 1 : q0);
-    auto mask = [&](int J) { return J < s.nb && J <= block_of(q1 - 1) ? mrow[J] : 0u; };
-    uint32_t w0 = mask(J0), w1 = mask(J0 + 1), w2 = mask(J0 + 2), w3 = mask(J0 + 3);
-    float cur[kBlock], nxt[kBlock];
-    int waited = 0;  // first of this warp's stages not yet observed complete
-    bool ok = nq <= 0 || __all_sync(0xffffffffu, tma::mbar_wait(&full[0], 0));
-    if (ok && nq > 0) {
-        if (q0 <= rb)
-            rs_rows(buf, lane, cur);
-        else
-            rs_cols(buf, lane, cur);
-        waited = 1;
-    }
-    for (int k = 0; ok && k < nq; ++k) {
-        const int q = q0 + k;
-        __syncwarp();  // every lane has stage k in registers: its buffer is free
-        if (lane == 0 && k + kRsStages < nq) {
-            tma::fence_proxy_async();
-            issue(k + kRsStages);
-        }
-        if (k + 1 < nq) {
-            const int st1 = (k + 1) % kRsStages;
-            ok = __all_sync(0xffffffffu, tma::mbar_wait(&full[st1], ((k + 1) / kRsStages) & 1));
-            if (ok) {
-                if (q + 1 <= rb)
-                    rs_rows(buf + st1 * kRsBox, lane, nxt);
-                else
-                    rs_cols(buf + st1 * kRsBox, lane, nxt);
-                waited = k + 2;
-            }
-        }
-#pragma unroll
-        for (int a = 0; a < kBlock; ++a) acc[a % kLanes].add(cur[a]);
-        if (q != rb) {  // partner block J complete (the diagonal after its B part): torque terms
-            const int J = block_of(q);
-            uint32_t wd = w0;
-            w0 = w1;
-            w1 = w2;
-            w2 = w3;
-            w3 = mask(J + 4);
-            while (wd) {
-                const int bit = __ffs(wd) - 1;
-                wd &= wd - 1;
-                aacc.add(trow[J * kBlock + bit]);
-            }
-        }
-#pragma unroll
-        for (int a = 0; a < kBlock; ++a) cur[a] = nxt[a];
-    }
-    if (!ok) {
-        const int issued = min(nq, waited + kRsStages);
-        for (int kk = waited; kk < issued; ++kk) tma::mbar_wait(&full[kk % kRsStages], (kk / kRsStages) & 1);
-        if (lane == 0) atomicOr(s.status, kStatusWaitTimeoutBit);
-    }
-    double fa = 0.0;
-#pragma unroll
-    for (int k = 0; k < kLanes; ++k) fa += f2d_bits(acc[k].s) + f2d_bits(acc[k].c);
-    double ta = f2d_bits(aacc.s) + f2d_bits(aacc.c);
-    if (SPLIT == 2) {  // both warps reach this barrier, failed or not
-        if (warp == 1) {
-            part[0][lane] = fa;
-            part[1][lane] = ta;
-            if (lane == 0) part_bad = ok ? 0 : 1;
-        }
-        __syncthreads();
-        if (warp == 1) return;
-        fa += part[0][lane];
-        ta += part[1][lane];
-        ok = ok && !part_bad;
-    }
-    if (!ok || i >= s.n) return;
-    s.acc.c[c][i] = fa;
-    s.aacc.c[c][i] = ta;
-    const double dt = s.sc->dt;
-    const double v = s.velh.c[c][i] + (.5 * fa) * dt;
-    const double wv = s.wh.c[c][i] + (.5 * ta) * dt;
-    s.vel.c[c][i] = v;
-    s.w.c[c][i] = wv;
-    if (!isfinite(v) || !isfinite(wv) || !isfinite(s.pos.c[c][i])) atomicOr(s.status, 1u);
-}
-
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
 {
     static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
@@ -428,28 +243,13 @@ bool make_map(const System& s, void* base, CUtensorMap* map)
 
 }  // namespace
 
-bool make_pair_map(const System& s, bool fp32_terms, CUtensorMap* map)
+bool make_pair_map(const System& s, CUtensorMap* map)
 {
-    if (!fp32_terms)
-        return make_map<double>(s, s.pairbuf, map) &&
-               cudaFuncSetAttribute(rowsum_tma_kernel<double, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    RsStage<1>::kSmem) == cudaSuccess &&
-               cudaFuncSetAttribute(rowsum_tma_kernel<double, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    RsStage<2>::kSmem) == cudaSuccess;
-    // the mixed form's tiles are contiguous: plain bulk copies, no tensor map
-    return cudaFuncSetAttribute(rowsum_mixed_kernel<kRsStages, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                MixShape<kRsStages>::kSmem) == cudaSuccess &&
-           cudaFuncSetAttribute(rowsum_mixed_kernel<kMixDeepStages, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                MixShape<kMixDeepStages>::kSmem) == cudaSuccess;
-}
-
-void launch_rowsum_mixed(const System& s, int num_sms, cudaStream_t st)
-{
-    if (3 * s.nb <= 4 * num_sms)  // every row block's CTA fits at 4 deep CTAs per SM: two warps per row block
-        rowsum_mixed_kernel<kMixDeepStages, 2><<<3 * s.nb, 32 * kRsWarps, MixShape<kMixDeepStages>::kSmem, st>>>(s);
-    else
-        rowsum_mixed_kernel<kRsStages, 1><<<(3 * s.nb + kRsWarps - 1) / kRsWarps, 32 * kRsWarps,
-                                            MixShape<kRsStages>::kSmem, st>>>(s);
+    return make_map<double>(s, s.pairbuf, map) &&
+           cudaFuncSetAttribute(rowsum_tma_kernel<double, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                RsStage<1>::kSmem) == cudaSuccess &&
+           cudaFuncSetAttribute(rowsum_tma_kernel<double, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                RsStage<2>::kSmem) == cudaSuccess;
 }
 
 template <typename T>

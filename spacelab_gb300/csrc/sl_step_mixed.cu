@@ -2,21 +2,36 @@
 //
 // More than FP32 is kept where precision is set:
 //   * FP64: positions and the whole integration (drift_kernel, shared with
-//     the exact form; pass 3 in the row sums), the previous-step distance
-//     test that chooses kin or kout, the write-step potential energy per
-//     pair and the energy totals;
+//     the exact form; pass 3 in mixed_finish_kernel), the previous-step
+//     distance test that chooses kin or kout, the write-step potential
+//     energy of near pairs and the energy totals (far pairs' vdW potential
+//     comes from a cancellation-free series in FP32, vdw_bracket_far);
 //   * double-float (hi + lo FP32 pairs, ~48 significant bits, sl_df.cuh):
-//     the pair subtraction r = pos[B] - pos[A] from double-float copies of
-//     the scaled positions, |r|^2 and the squared gap
-//     g = (R_A + R_B)^2 - |r|^2, from which the overlap is taken as
-//     g / (R_A + R_B + |r|) -- no cancellation in R_A + R_B - |r|; and the
-//     per-sphere sums of the FP32 pair terms (compensated, in ascending
-//     partner order, then converted to FP64).
+//     for pairs closer than twice the sum of their radii, the subtraction
+//     r = pos[B] - pos[A] from double-float copies of the scaled positions,
+//     |r|^2 and the squared gap g = (R_A + R_B)^2 - |r|^2, from which the
+//     overlap is taken as g / (R_A + R_B + |r|) -- no cancellation in
+//     R_A + R_B - |r|; and the per-sphere sums of the partial sums
+//     (compensated, then converted to FP64).
 // Everything else -- distances, the vdW coefficient, elastic, gravity,
 // sliding and rolling friction, torques -- is FP32 on lengths scaled by
 // 2^-len_shift (about one radius), which keeps R^6 / (S^2 T^2) far from
-// FP32's range limits.  The non-contact pair path thus issues no FP64
-// instruction: GB300's FP32 pipe is ~72x its FP64 pipe.
+// FP32's range limits.  A pair at least twice its radii sum apart has a gap
+// h >= R_A + R_B, so FP32 geometry (r from the hi and lo parts, |r| from
+// rsqrt) keeps h to a few ulp: such pairs, nearly all of them, take a short
+// FP32-only path.  No pair issues an FP64 instruction outside the contact
+// branch and write steps: GB300's FP32 pipe is ~72x its FP64 pipe.
+//
+// Accumulation: the pair terms never reach memory.  A warp evaluates a
+// 32 x 32 tile in a diagonal sweep -- at step k, lane b takes pair
+// (row (b + k) mod 32, column b) -- so that each lane adds its column
+// sphere's terms in a register and each row's running sum travels one lane
+// down per step (one shuffle per component) to meet its next term; after
+// the 32 steps lane l holds row l's sum.  The tile then writes one FP32
+// partial per sphere and component, and mixed_finish_kernel adds a sphere's
+// partials over the partner blocks in ascending order in compensated sums.
+// Every order is fixed, so runs repeat bit for bit.
+//
 // The physics follows ColliderSingleCore.cpp:104-253 term by term; only the
 // arithmetic and the evaluation order differ.
 #include "sl_device.cuh"
@@ -28,10 +43,13 @@ namespace sl {
 
 namespace {
 
-struct ABlockMixed {
-    float p[6][kBlock];  // scaled position hi (x, y, z), then lo (x, y, z)
-    float Rs[kBlock], Rlo[kBlock], inv_m[kBlock];
-};
+// Row spheres of a tile in shared memory, kRowStride floats each, so that a
+// warp's 16-byte loads of 32 different rows fall in distinct banks:
+//   [0..3] scaled position hi x, y, z and scaled radius R,
+//   [4..7] scaled position lo x, y, z and c_vdw R^3,
+//   [8] the radius's lo part, [9] 1/m.
+constexpr int kRowStride = 12;
+constexpr int kPairWarps = 4;
 
 // |pos[B] - pos[A]|^2 in FP64, the formula of the previous-step distance in
 // contact_mixed (rare paths: the contact test, write-step energies).
@@ -43,75 +61,91 @@ __device__ __forceinline__ double fp64_d2(const System& s, int A, int B)
     return fma(rx, rx, fma(ry, ry, rz * rz));
 }
 
-// Same tiling as pair_tile_kernel: one warp per lower-triangular 32x32 block
-// tile, lane b = sphere 32Y+b, loop over the A block; terms stored as FP32:
-// sphere A's in the A-side buffer (the float view of pairbuf), sphere B's in
-// the B-side buffer pairT, both at mixed_term_index(A, B): tile (X, Y) of
-// both is 4 KB of contiguous memory and each of a warp's stores covers one
-// 128-byte row of it.  Torques (contacts only) go to the float view of
-// torqbuf, [A][B] and [B][A].
+// One warp per lower-triangular 32 x 32 block tile (X, Y), X >= Y: column
+// lane b is sphere B = 32Y + b, row r is sphere A = 32X + r (A > B).  Writes
+// the tile's partials f_part[c][Y][A] (sphere A's terms from block Y) and
+// f_part[c][X][B] (sphere B's from block X), or on the diagonal one partial
+// f_part[c][X][i] with both; contact bits to cmask[K][i]; torques of contacts
+// to the float view of torqbuf, [A][B] and [B][A].
 template <bool WRITE>
-__global__ void __launch_bounds__(128, 4) mixed_pair_kernel(const __grid_constant__ System s)
+__global__ void __launch_bounds__(32 * kPairWarps, 4) mixed_pair_kernel(const __grid_constant__ System s)
 {
-    __shared__ ABlockMixed sA[4];
+    __shared__ __align__(16) float rows_all[kPairWarps][kBlock * kRowStride];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
-    ABlockMixed& ab = sA[wib];
-    const long long nwarps = (long long)gridDim.x * 4;
-    const size_t plane = (size_t)s.npad * s.npad;
-    float* pbuf = reinterpret_cast<float*>(s.pairbuf);
+    float* rows = rows_all[wib];
+    const long long nwarps = (long long)gridDim.x * kPairWarps;
+    const size_t plane = (size_t)s.npad * s.npad;  // torque planes
+    const size_t pplane = (size_t)s.nb * s.npad;   // partial planes
     float* tbuf = reinterpret_cast<float*>(s.torqbuf);
     const int sh = s.len_shift;
     const float L = ldexpf(1.0f, sh);
     const float hmin_s = (float)s.mat.h_min / L;
     const float c_vdw = (float)(s.mat.Ha / 6 * 64) / L;   // dyn per unit vdw_shape
+    const int nxt = (lane + 1) & (kBlock - 1);
 
-    for (long long t = (long long)blockIdx.x * 4 + wib; t < s.ntiles; t += nwarps) {
+    for (long long t = (long long)blockIdx.x * kPairWarps + wib; t < s.ntiles; t += nwarps) {
         int X, Y;
         tile_coords(t, X, Y);
         {
-            const int i = X * kBlock + lane;
-#pragma unroll
-            for (int k = 0; k < 6; ++k) ab.p[k][lane] = s.f_pos[k][i];
-            ab.Rs[lane] = s.f_R[i]; ab.Rlo[lane] = s.f_Rlo[i]; ab.inv_m[lane] = s.f_inv_m[i];
+            const int i = X * kBlock + lane;  // < npad
+            const float Ri = s.f_R[i];
+            float* row = rows + lane * kRowStride;
+            *reinterpret_cast<float4*>(row) = make_float4(s.f_pos[0][i], s.f_pos[1][i], s.f_pos[2][i], Ri);
+            *reinterpret_cast<float4*>(row + 4) =
+                make_float4(s.f_pos[3][i], s.f_pos[4][i], s.f_pos[5][i], c_vdw * (Ri * Ri * Ri));
+            row[8] = s.f_Rlo[i];
+            row[9] = s.f_inv_m[i];
         }
         __syncwarp();
         const int B = Y * kBlock + lane;
         const bool bvalid = B < s.n;
-        float bp[6];
-#pragma unroll
-        for (int k = 0; k < 6; ++k) bp[k] = s.f_pos[k][B];
+        const float bx = s.f_pos[0][B], by = s.f_pos[1][B], bz = s.f_pos[2][B];
+        const float bxl = s.f_pos[3][B], byl = s.f_pos[4][B], bzl = s.f_pos[5][B];
         const float Rbs = s.f_R[B], Rblo = s.f_Rlo[B], inv_mb = s.f_inv_m[B];
-        const int a_end = min(kBlock, s.n - X * kBlock);
+        const float Rb3 = Rbs * Rbs * Rbs;
+        const int nA = s.n - X * kBlock;  // rows r < nA are spheres
         double pe = 0;
-        uint32_t rowbits = 0, colbits = 0;
-        // tile (X, Y) of both term buffers; element (a, lane) of row a is at
-        // a * 32 + swizzled lane, so a warp's store covers one 128-byte row
-        const size_t tile = ((size_t)X * s.nb + Y) * 1024;
-        float* tileA = pbuf + tile;
-        float* tileT = s.pairT + tile;
-        for (int a = 0; a < a_end; ++a) {
-            const bool valid = bvalid && (X != Y || lane < a);
+        df::Sum pe_far{0.0f, 0.0f};  // far pairs' vdW brackets (write steps)
+        uint32_t colbits = 0;
+        float ax = 0, ay = 0, az = 0;     // running sum of row (lane + k) mod 32 at step k
+        float bsx = 0, bsy = 0, bsz = 0;  // sphere B's sum
+        for (int k = 0; k < kBlock; ++k) {
+            const int r = (lane + k) & (kBlock - 1);
+            const bool valid = bvalid && r < nA && (X != Y || lane < r);
+            const float4 q0 = *reinterpret_cast<const float4*>(rows + r * kRowStride);
+            const float4 q1 = *reinterpret_cast<const float4*>(rows + r * kRowStride + 4);
+            const float Ras = q0.w;
+            // FP32 geometry (scaled lengths), exact for far pairs to a few ulp
+            const float rx = (bx - q0.x) + (bxl - q1.x);
+            const float ry = (by - q0.y) + (byl - q1.y);
+            const float rz = (bz - q0.z) + (bzl - q1.z);
+            const float d2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
+            const float sumR = Ras + Rbs;
+            const float inv_d = rsqrtf(d2);
+            // vdW (:205-226) at gap h = |r| - R_A - R_B: Ra^3 Rb^3 (h+Ra+Rb) / (S^2 T^2)
+            const float h = fmaxf(fmaf(d2, inv_d, -sumR), hmin_s);
+            const float S = h * (h + 2.0f * sumR);
+            const float T = fmaf(4.0f * Ras, Rbs, S);
+            const float fr = __fdividef((q1.w * Rb3) * (h + sumR), (S * S) * (T * T)) * inv_d;  // |F| / |r|
+            float fx = fr * rx, fy = fr * ry, fz = fr * rz;
             bool contact = false;
-            if (valid) {
-                const int A = X * kBlock + a;
-                // double-float (~48 bits, FP32 pipe): subtraction, |r|^2 and
-                // the squared gap g = (R_A + R_B)^2 - |r|^2, in scaled lengths
-                const df::F2 rx = df::sub({bp[0], bp[3]}, {ab.p[0][a], ab.p[3][a]});
-                const df::F2 ry = df::sub({bp[1], bp[4]}, {ab.p[1][a], ab.p[4][a]});
-                const df::F2 rz = df::sub({bp[2], bp[5]}, {ab.p[2][a], ab.p[5][a]});
-                const df::F2 d2 = df::add(df::add(df::sqr(rx), df::sqr(ry)), df::sqr(rz));
-                const float Ras = ab.Rs[a];
-                const df::F2 sum = df::add({Ras, ab.Rlo[a]}, {Rbs, Rblo});
-                const df::F2 gap2 = df::sub(df::sqr(sum), d2);
-                // FP32 (scaled lengths)
-                const float rxs = rx.hi, rys = ry.hi, rzs = rz.hi;
-                const float d2s = d2.hi;
-                const float inv_d = rsqrtf(d2s);
-                const float dist_s = d2s * inv_d;
+            const bool nearp = d2 < 4.0f * sumR * sumR;
+            if (valid && nearp) {
+                // near pair: double-float (~48 bits, FP32 pipe) subtraction,
+                // |r|^2 and squared gap g = (R_A + R_B)^2 - |r|^2
+                const int A = X * kBlock + r;
+                const df::F2 drx = df::sub({bx, bxl}, {q0.x, q1.x});
+                const df::F2 dry = df::sub({by, byl}, {q0.y, q1.y});
+                const df::F2 drz = df::sub({bz, bzl}, {q0.z, q1.z});
+                const df::F2 dd2 = df::add(df::add(df::sqr(drx), df::sqr(dry)), df::sqr(drz));
+                const df::F2 sum = df::add({Ras, rows[r * kRowStride + 8]}, {Rbs, Rblo});
+                const df::F2 gap2 = df::sub(df::sqr(sum), dd2);
+                const float d2s = dd2.hi;
+                const float inv_dn = rsqrtf(d2s);
+                const float dist_s = d2s * inv_dn;
                 const float ovl_s = __fdividef(gap2.hi, Ras + Rbs + dist_s);
-                const float nx = rxs * inv_d, ny = rys * inv_d, nz = rzs * inv_d;
-                float fx, fy, fz;
+                const float nx = drx.hi * inv_dn, ny = dry.hi * inv_dn, nz = drz.hi * inv_dn;
                 if (gap2.hi > 0.0f || (gap2.hi == 0.0f && gap2.lo > 0.0f)) {
                     contact = true;
                     const ContactIn in = gather_contact(s, A, B);
@@ -131,32 +165,55 @@ __global__ void __launch_bounds__(128, 4) mixed_pair_kernel(const __grid_constan
                         pe += pair_pe_fp64(s.mat, s.R[A], s.R[B], fma(sum64, sum64, -d2_64), d2_64, true, o.k);
                     }
                 } else {
-                    const float h = fmaxf(-ovl_s, hmin_s);                  // :211-215
-                    const float f = c_vdw * vdw_shape(h, Ras, Rbs);
+                    const float hn = fmaxf(-ovl_s, hmin_s);                 // :211-215
+                    const float f = c_vdw * vdw_shape(hn, Ras, Rbs);
                     fx = f * nx; fy = f * ny; fz = f * nz;
-                    if (WRITE) {  // write steps only: the FP64 geometry, as the contact branch
-                        const double d2_64 = fp64_d2(s, A, B), sum64 = s.R[A] + s.R[B];
-                        pe += pair_pe_fp64(s.mat, s.R[A], s.R[B], fma(sum64, sum64, -d2_64), d2_64, false, 0.0);
-                    }
                 }
-                const float ima = ab.inv_m[a];
-                const int e = a * 32 + ((((lane >> 2) ^ (a & 7)) << 2) | (lane & 3));  // mixed_term_index
-                float* pa = tileA + e;
-                __stcs(pa, fx * ima); __stcs(pa + plane, fy * ima); __stcs(pa + 2 * plane, fz * ima);
-                float* pb = tileT + e;
-                __stcs(pb, -fx * inv_mb); __stcs(pb + plane, -fy * inv_mb); __stcs(pb + 2 * plane, -fz * inv_mb);
             }
-            const uint32_t bal = __ballot_sync(0xffffffffu, contact);
-            if (lane == a) rowbits = bal;
-            if (contact) colbits |= 1u << a;
+            if (WRITE && valid && !contact) {  // write steps only
+                if (nearp) {  // the FP64 geometry, as the contact branch
+                    const int A = X * kBlock + r;
+                    const double d2_64 = fp64_d2(s, A, B), sum64 = s.R[A] + s.R[B];
+                    pe += pair_pe_fp64(s.mat, s.R[A], s.R[B], fma(sum64, sum64, -d2_64), d2_64, false, 0.0);
+                } else {
+                    pe_far.add(vdw_bracket_far(d2, Ras, Rbs));
+                }
+            }
+            if (!valid) fx = fy = fz = 0.0f;
+            ax += fx; ay += fy; az += fz;
+            bsx += fx; bsy += fy; bsz += fz;
+            if (contact) colbits |= 1u << r;
+            ax = __shfl_sync(0xffffffffu, ax, nxt);
+            ay = __shfl_sync(0xffffffffu, ay, nxt);
+            az = __shfl_sync(0xffffffffu, az, nxt);
         }
-        if (X == Y) {
-            s.cmask[(size_t)(X * kBlock + lane) * s.nb + X] = rowbits | colbits;
+        // lane l now holds row l's sum; its contact bits are the transpose of
+        // the lanes' column bits
+        uint32_t rowbits = 0;
+        if (__any_sync(0xffffffffu, colbits != 0u)) {
+            for (int r = 0; r < kBlock; ++r) {
+                const uint32_t wd = __ballot_sync(0xffffffffu, (colbits >> r) & 1u);
+                if (lane == r) rowbits = wd;
+            }
+        }
+        const int iA = X * kBlock + lane;
+        const float ima = rows[lane * kRowStride + 9];
+        float* P = s.f_part;
+        if (X == Y) {  // sphere iA == B: partners j < i as A (row), j > i as B (column)
+            const size_t o = (size_t)X * s.npad + iA;
+            P[o] = fmaf(ima, ax, -inv_mb * bsx);
+            P[o + pplane] = fmaf(ima, ay, -inv_mb * bsy);
+            P[o + 2 * pplane] = fmaf(ima, az, -inv_mb * bsz);
+            s.cmask[o] = rowbits | colbits;
         } else {
-            s.cmask[(size_t)(X * kBlock + lane) * s.nb + Y] = rowbits;
-            s.cmask[(size_t)(Y * kBlock + lane) * s.nb + X] = colbits;
+            const size_t oa = (size_t)Y * s.npad + iA, ob = (size_t)X * s.npad + B;
+            P[oa] = ima * ax; P[oa + pplane] = ima * ay; P[oa + 2 * pplane] = ima * az;
+            P[ob] = -inv_mb * bsx; P[ob + pplane] = -inv_mb * bsy; P[ob + 2 * pplane] = -inv_mb * bsz;
+            s.cmask[oa] = rowbits;
+            s.cmask[ob] = colbits;
         }
         if (WRITE) {
+            pe += -s.mat.Ha / 6 * (f2d_bits(pe_far.s) + f2d_bits(pe_far.c));
             for (int off = 16; off > 0; off >>= 1) pe += __shfl_xor_sync(0xffffffffu, pe, off);
             if (lane == 0) s.pe_tile[t] = pe;
         }
@@ -164,64 +221,109 @@ __global__ void __launch_bounds__(128, 4) mixed_pair_kernel(const __grid_constan
     }
 }
 
-constexpr int kMixThreads = 32;
+constexpr int kFinSlices = 8;
 
-// Plain-load form of the row sums (used only when no tensor map could be
-// made): thread (c, i) sums the FP32 terms of sphere i in FP64 in ascending
-// partner order, torque terms of contact partners likewise, then pass 3.
-__global__ void __launch_bounds__(kMixThreads) mixed_rowsum_kernel(const __grid_constant__ System s)
+// Per-sphere totals, then pass 3.  Block = 32 spheres (lanes) x kFinSlices
+// warps; warp w adds partner blocks [nb w / S, nb (w+1) / S) of its lane's
+// sphere: the force partials f_part[c][K][i] in compensated double-float sums
+// (coalesced loads along i), and the torque terms of contact partners (bits
+// of cmask[K][i], ascending) in FP64.  Warp 0 adds the slices in order and
+// integrates (ColliderSingleCore.cpp:263-267).
+__global__ void __launch_bounds__(32 * kFinSlices) mixed_finish_kernel(const __grid_constant__ System s)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= 3 * s.n) return;
-    const int c = t / s.n;
-    const int i = t - c * s.n;
-    const int n = s.n;
+    __shared__ float fs[kFinSlices][6][kBlock];
+    __shared__ double ts[kFinSlices][3][kBlock];
+    const int lane = threadIdx.x & 31;
+    const int w = threadIdx.x >> 5;
+    const int i = blockIdx.x * kBlock + lane;  // < npad
+    const int K0 = (int)((long long)s.nb * w / kFinSlices);
+    const int K1 = (int)((long long)s.nb * (w + 1) / kFinSlices);
+    const size_t pplane = (size_t)s.nb * s.npad;
     const size_t plane = (size_t)s.npad * s.npad;
-    // partners j < i from the A side (i, j), j > i from the B side (j, i)
-    const float* pA = reinterpret_cast<const float*>(s.pairbuf) + c * plane;
-    const float* pT = s.pairT + c * plane;
-    double acc = 0.0;
-    for (int j = 0; j < i; ++j) acc += f2d_bits(__ldcs(pA + mixed_term_index(s.nb, i, j)));
-    for (int j = i + 1; j < n; ++j) acc += f2d_bits(__ldcs(pT + mixed_term_index(s.nb, j, i)));
-    double aacc = 0.0;
-    const uint32_t* mrow = s.cmask + (size_t)i * s.nb;
-    const float* trow = reinterpret_cast<const float*>(s.torqbuf) + c * plane + (size_t)i * s.npad;
-    for (int Y = 0; Y < s.nb; ++Y) {
-        uint32_t wd = mrow[Y];
+    const float* p = s.f_part + i;
+    const uint32_t* mk = s.cmask + i;
+    const float* tb = reinterpret_cast<const float*>(s.torqbuf) + (size_t)i * s.npad;
+    df::Sum fx{0.0f, 0.0f}, fy{0.0f, 0.0f}, fz{0.0f, 0.0f};
+    double tx = 0, ty = 0, tz = 0;
+    auto torques = [&](uint32_t wd, int K) {
         while (wd) {
-            const int b = __ffs(wd) - 1;
+            const int j = K * kBlock + __ffs(wd) - 1;
             wd &= wd - 1;
-            aacc += f2d_bits(trow[Y * kBlock + b]);
+            tx += f2d_bits(tb[j]);
+            ty += f2d_bits(tb[j + plane]);
+            tz += f2d_bits(tb[j + 2 * plane]);
+        }
+    };
+    constexpr int U = 4;
+    int K = K0;
+    for (; K + U <= K1; K += U) {
+        float vx[U], vy[U], vz[U];
+        uint32_t m[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const size_t o = (size_t)(K + u) * s.npad;
+            vx[u] = __ldcs(p + o);
+            vy[u] = __ldcs(p + o + pplane);
+            vz[u] = __ldcs(p + o + 2 * pplane);
+            m[u] = __ldcs(mk + o);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            fx.add(vx[u]);
+            fy.add(vy[u]);
+            fz.add(vz[u]);
+            torques(m[u], K + u);
         }
     }
+    for (; K < K1; ++K) {
+        const size_t o = (size_t)K * s.npad;
+        fx.add(__ldcs(p + o));
+        fy.add(__ldcs(p + o + pplane));
+        fz.add(__ldcs(p + o + 2 * pplane));
+        torques(__ldcs(mk + o), K);
+    }
+    fs[w][0][lane] = fx.s; fs[w][1][lane] = fx.c;
+    fs[w][2][lane] = fy.s; fs[w][3][lane] = fy.c;
+    fs[w][4][lane] = fz.s; fs[w][5][lane] = fz.c;
+    ts[w][0][lane] = tx; ts[w][1][lane] = ty; ts[w][2][lane] = tz;
+    __syncthreads();
+    if (w != 0 || i >= s.n) return;
     const double dt = s.sc->dt;
-    const double v = s.velh.c[c][i] + (.5 * acc) * dt;
-    const double wv = s.wh.c[c][i] + (.5 * aacc) * dt;
-    s.acc.c[c][i] = acc;
-    s.aacc.c[c][i] = aacc;
-    s.vel.c[c][i] = v;
-    s.w.c[c][i] = wv;
-    if (!isfinite(v) || !isfinite(wv) || !isfinite(s.pos.c[c][i])) atomicOr(s.status, 1u);
+    bool bad = false;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        double acc = 0, aacc = 0;
+#pragma unroll
+        for (int ww = 0; ww < kFinSlices; ++ww) {
+            acc += f2d_bits(fs[ww][2 * c][lane]) + f2d_bits(fs[ww][2 * c + 1][lane]);
+            aacc += ts[ww][c][lane];
+        }
+        const double v = s.velh.c[c][i] + (.5 * acc) * dt;    // :265
+        const double wv = s.wh.c[c][i] + (.5 * aacc) * dt;   // :266
+        s.acc.c[c][i] = acc;
+        s.aacc.c[c][i] = aacc;
+        s.vel.c[c][i] = v;
+        s.w.c[c][i] = wv;
+        bad = bad || !isfinite(v) || !isfinite(wv) || !isfinite(s.pos.c[c][i]);
+    }
+    if (bad) atomicOr(s.status, 1u);
 }
 
 }  // namespace
 
-void launch_step_mixed(const System& s, bool write, int num_sms, cudaStream_t st, StepTimers* tm, bool bulk_rows)
+void launch_step_mixed(const System& s, bool write, int num_sms, cudaStream_t st, StepTimers* tm)
 {
     launch_drift(s, st);
     if (tm) cudaEventRecord(tm->ev[0], st);
-    long long want = (s.ntiles + 3) / 4;
+    long long want = (s.ntiles + kPairWarps - 1) / kPairWarps;
     long long cap = (long long)num_sms * 4;  // 4 CTAs (16 warps) per SM
     const int pb = (int)(want < cap ? want : cap);
     if (write)
-        mixed_pair_kernel<true><<<pb, 128, 0, st>>>(s);
+        mixed_pair_kernel<true><<<pb, 32 * kPairWarps, 0, st>>>(s);
     else
-        mixed_pair_kernel<false><<<pb, 128, 0, st>>>(s);
+        mixed_pair_kernel<false><<<pb, 32 * kPairWarps, 0, st>>>(s);
     if (tm) cudaEventRecord(tm->ev[1], st);
-    if (bulk_rows)
-        launch_rowsum_mixed(s, num_sms, st);
-    else
-        mixed_rowsum_kernel<<<(3 * s.n + kMixThreads - 1) / kMixThreads, kMixThreads, 0, st>>>(s);
+    mixed_finish_kernel<<<s.nb, 32 * kFinSlices, 0, st>>>(s);
     if (tm) cudaEventRecord(tm->ev[2], st);
     if (write) launch_energy(s, st);
 }
