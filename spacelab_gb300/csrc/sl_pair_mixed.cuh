@@ -21,18 +21,26 @@ __device__ __forceinline__ float vdw_shape(float h, float Ra, float Rb)
     return __fdividef(r3 * (h + sum), (S * S) * (T * T));
 }
 
+// Approximate FP32 reciprocal (one MUFU instruction, relative error below
+// 2^-22; subnormal inputs and results flush to zero).
+__device__ __forceinline__ float rcp_approx(float x)
+{
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 // The vdW potential's bracket 2RaRb/P + 2RaRb/Q + ln(P/Q), P = z^2 - (Ra+Rb)^2,
 // Q = z^2 - (Ra-Rb)^2 (ColliderSingleCore.cpp:228-240; U = -Ha/6 times it),
-// for a pair at centre distance z >= 2 (Ra + Rb), from d2 = z^2 in scaled
-// lengths.  With u = 4 Ra Rb / Q (P/Q = 1 - u) the bracket is
+// for a pair at centre distance z >= 2 (Ra + Rb), from Q in scaled lengths.
+// With u = 4 Ra Rb / Q (P/Q = 1 - u) the bracket is
 // u/(2(1-u)) + u/2 + ln(1-u) = sum_{k>=3} (k-2)/(2k) u^k: its O(u) and
 // O(u^2) parts cancel exactly, which the closed form resolves only in FP64.
 // Here u <= 1/4, so the terms up to k = 15 leave a relative truncation
 // error below 5e-8, and FP32 Horner evaluation suffices.
-__device__ __forceinline__ float vdw_bracket_far(float d2, float Ra, float Rb)
+__device__ __forceinline__ float vdw_bracket_far(float Q, float Ra, float Rb)
 {
-    const float dd = Ra - Rb;
-    const float u = __fdividef(4.0f * Ra * Rb, fmaf(-dd, dd, d2));
+    const float u = (4.0f * Ra * Rb) * rcp_approx(Q);
     float p = 13.0f / 30.0f;                 // k = 15
     p = fmaf(p, u, 3.0f / 7.0f);             // 14
     p = fmaf(p, u, 11.0f / 26.0f);           // 13

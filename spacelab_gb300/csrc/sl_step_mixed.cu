@@ -17,9 +17,9 @@
 // sliding and rolling friction, torques -- is FP32 on lengths scaled by
 // 2^-len_shift (about one radius), which keeps R^6 / (S^2 T^2) far from
 // FP32's range limits.  A pair at least twice its radii sum apart has a gap
-// h >= R_A + R_B, so FP32 geometry (r from the hi and lo parts, |r| from
-// rsqrt) keeps h to a few ulp: such pairs, nearly all of them, take a short
-// FP32-only path.  No pair issues an FP64 instruction outside the contact
+// h >= R_A + R_B, so FP32 geometry (r from the hi and lo parts) keeps
+// |r|^2 - (R_A +- R_B)^2 to a few ulp, and its vdW force needs no square
+// root: such pairs, nearly all of them, take a short FP32-only path.  No pair issues an FP64 instruction outside the contact
 // branch and write steps: GB300's FP32 pipe is ~72x its FP64 pipe.
 //
 // Accumulation: the pair terms never reach memory.  A warp evaluates a
@@ -38,6 +38,8 @@
 #include "sl_kernels.h"
 #include "sl_df.cuh"
 #include "sl_pair_mixed.cuh"
+
+#include <type_traits>
 
 namespace sl {
 
@@ -83,6 +85,26 @@ __global__ void __launch_bounds__(32 * kPairWarps, 4) mixed_pair_kernel(const __
     const float hmin_s = (float)s.mat.h_min / L;
     const float c_vdw = (float)(s.mat.Ha / 6 * 64) / L;   // dyn per unit vdw_shape
     const int nxt = (lane + 1) & (kBlock - 1);
+    // write steps: near pairs out of contact whose FP64 potential is pending.
+    // Their FP64 evaluation runs with every lane busy (the FP64 pipe takes a
+    // warp instruction per ~64 cycles however few lanes are active)
+    __shared__ int2 queue_all[WRITE ? kPairWarps : 1][WRITE ? 2 * kBlock : 1];
+    int2* q = queue_all[WRITE ? wib : 0];
+    int qn = 0;
+    double pe = 0;
+    auto flush_near = [&](int cnt) {  // pairs q[0 .. cnt), cnt <= 32; the rest move down
+        if (lane < cnt) {
+            const int A = q[lane].x, B = q[lane].y;
+            const double d2_64 = fp64_d2(s, A, B), sum64 = s.R[A] + s.R[B];
+            pe += pair_pe_fp64(s.mat, s.R[A], s.R[B], fma(sum64, sum64, -d2_64), d2_64, false, 0.0);
+        }
+        const int left = qn - cnt;
+        const int2 e = lane < left ? q[cnt + lane] : make_int2(0, 0);
+        __syncwarp();
+        if (lane < left) q[lane] = e;
+        __syncwarp();
+        qn = left;
+    };
 
     for (long long t = (long long)blockIdx.x * kPairWarps + wib; t < s.ntiles; t += nwarps) {
         int X, Y;
@@ -105,88 +127,104 @@ __global__ void __launch_bounds__(32 * kPairWarps, 4) mixed_pair_kernel(const __
         const float Rbs = s.f_R[B], Rblo = s.f_Rlo[B], inv_mb = s.f_inv_m[B];
         const float Rb3 = Rbs * Rbs * Rbs;
         const int nA = s.n - X * kBlock;  // rows r < nA are spheres
-        double pe = 0;
+        pe = 0;
         df::Sum pe_far{0.0f, 0.0f};  // far pairs' vdW brackets (write steps)
         uint32_t colbits = 0;
         float ax = 0, ay = 0, az = 0;     // running sum of row (lane + k) mod 32 at step k
         float bsx = 0, bsy = 0, bsz = 0;  // sphere B's sum
-        for (int k = 0; k < kBlock; ++k) {
-            const int r = (lane + k) & (kBlock - 1);
-            const bool valid = bvalid && r < nA && (X != Y || lane < r);
-            const float4 q0 = *reinterpret_cast<const float4*>(rows + r * kRowStride);
-            const float4 q1 = *reinterpret_cast<const float4*>(rows + r * kRowStride + 4);
-            const float Ras = q0.w;
-            // FP32 geometry (scaled lengths), exact for far pairs to a few ulp
-            const float rx = (bx - q0.x) + (bxl - q1.x);
-            const float ry = (by - q0.y) + (byl - q1.y);
-            const float rz = (bz - q0.z) + (bzl - q1.z);
-            const float d2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
-            const float sumR = Ras + Rbs;
-            const float inv_d = rsqrtf(d2);
-            // vdW (:205-226) at gap h = |r| - R_A - R_B: Ra^3 Rb^3 (h+Ra+Rb) / (S^2 T^2)
-            const float h = fmaxf(fmaf(d2, inv_d, -sumR), hmin_s);
-            const float S = h * (h + 2.0f * sumR);
-            const float T = fmaf(4.0f * Ras, Rbs, S);
-            const float fr = __fdividef((q1.w * Rb3) * (h + sumR), (S * S) * (T * T)) * inv_d;  // |F| / |r|
-            float fx = fr * rx, fy = fr * ry, fz = fr * rz;
-            bool contact = false;
-            const bool nearp = d2 < 4.0f * sumR * sumR;
-            if (valid && nearp) {
-                // near pair: double-float (~48 bits, FP32 pipe) subtraction,
-                // |r|^2 and squared gap g = (R_A + R_B)^2 - |r|^2
-                const int A = X * kBlock + r;
-                const df::F2 drx = df::sub({bx, bxl}, {q0.x, q1.x});
-                const df::F2 dry = df::sub({by, byl}, {q0.y, q1.y});
-                const df::F2 drz = df::sub({bz, bzl}, {q0.z, q1.z});
-                const df::F2 dd2 = df::add(df::add(df::sqr(drx), df::sqr(dry)), df::sqr(drz));
-                const df::F2 sum = df::add({Ras, rows[r * kRowStride + 8]}, {Rbs, Rblo});
-                const df::F2 gap2 = df::sub(df::sqr(sum), dd2);
-                const float d2s = dd2.hi;
-                const float inv_dn = rsqrtf(d2s);
-                const float dist_s = d2s * inv_dn;
-                const float ovl_s = __fdividef(gap2.hi, Ras + Rbs + dist_s);
-                const float nx = drx.hi * inv_dn, ny = dry.hi * inv_dn, nz = drz.hi * inv_dn;
-                if (gap2.hi > 0.0f || (gap2.hi == 0.0f && gap2.lo > 0.0f)) {
-                    contact = true;
-                    const ContactIn in = gather_contact(s, A, B);
-                    // the kin/kout test compares |r|^2 with the previous step's,
-                    // both in FP64 from the FP64 positions with one formula
-                    const double d2_64 = fp64_d2(s, A, B);
-                    const ContactF o = contact_mixed(in, s.mat, sh, d2_64, nx, ny, nz, dist_s * L, ovl_s * L, Ras,
-                                                     Rbs);
-                    fx = o.fx; fy = o.fy; fz = o.fz;
-                    const float ima = s.f_inv_moi[A], imb = s.f_inv_moi[B];
-                    float* ta = tbuf + (size_t)A * s.npad + B;
-                    float* tb = tbuf + (size_t)B * s.npad + A;
-                    ta[0] = o.tax * ima; ta[plane] = o.tay * ima; ta[2 * plane] = o.taz * ima;
-                    tb[0] = o.tbx * imb; tb[plane] = o.tby * imb; tb[2 * plane] = o.tbz * imb;
-                    if (WRITE) {
-                        const double sum64 = s.R[A] + s.R[B];
-                        pe += pair_pe_fp64(s.mat, s.R[A], s.R[B], fma(sum64, sum64, -d2_64), d2_64, true, o.k);
-                    }
-                } else {
-                    const float hn = fmaxf(-ovl_s, hmin_s);                 // :211-215
-                    const float f = c_vdw * vdw_shape(hn, Ras, Rbs);
-                    fx = f * nx; fy = f * ny; fz = f * nz;
-                }
-            }
-            if (WRITE && valid && !contact) {  // write steps only
-                if (nearp) {  // the FP64 geometry, as the contact branch
+        // FULL: a tile off the diagonal whose rows and columns are all spheres
+        auto sweep = [&](auto full_tag) {
+            constexpr bool FULL = decltype(full_tag)::value;
+#pragma unroll 2
+            for (int k = 0; k < kBlock; ++k) {
+                const int r = (lane + k) & (kBlock - 1);
+                const bool valid = FULL || (bvalid && r < nA && (X != Y || lane < r));
+                const float4 q0 = *reinterpret_cast<const float4*>(rows + r * kRowStride);
+                const float4 q1 = *reinterpret_cast<const float4*>(rows + r * kRowStride + 4);
+                const float Ras = q0.w;
+                // far pairs, |r| >= 2 (R_A + R_B), in FP32 (scaled lengths): the
+                // gap h = |r| - R_A - R_B is then at least R_A + R_B, so the vdW
+                // force (:205-226) Ra^3 Rb^3 (h + Ra + Rb) / (S^2 T^2) along r/|r|
+                // needs no square root: h + Ra + Rb = |r|, S = h (h + 2(Ra + Rb))
+                // = |r|^2 - (Ra + Rb)^2 and T = S + 4 Ra Rb = |r|^2 - (Ra - Rb)^2,
+                // neither cancelling by more than a quarter
+                const float rx = (bx - q0.x) + (bxl - q1.x);
+                const float ry = (by - q0.y) + (byl - q1.y);
+                const float rz = (bz - q0.z) + (bzl - q1.z);
+                const float d2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
+                const float sumR = Ras + Rbs, difR = Ras - Rbs;
+                const float sum2 = sumR * sumR;
+                const float S = d2 - sum2;
+                const float T = fmaf(-difR, difR, d2);
+                const float P = S * T;
+                const float fr = (q1.w * Rb3) * rcp_approx(P * P);  // |F| / |r|
+                float fx = fr * rx, fy = fr * ry, fz = fr * rz;
+                bool contact = false;
+                const bool nearp = d2 < 4.0f * sum2;
+                if (valid && nearp) {
+                    // near pair: double-float (~48 bits, FP32 pipe) subtraction,
+                    // |r|^2 and squared gap g = (R_A + R_B)^2 - |r|^2
                     const int A = X * kBlock + r;
-                    const double d2_64 = fp64_d2(s, A, B), sum64 = s.R[A] + s.R[B];
-                    pe += pair_pe_fp64(s.mat, s.R[A], s.R[B], fma(sum64, sum64, -d2_64), d2_64, false, 0.0);
-                } else {
-                    pe_far.add(vdw_bracket_far(d2, Ras, Rbs));
+                    const df::F2 drx = df::sub({bx, bxl}, {q0.x, q1.x});
+                    const df::F2 dry = df::sub({by, byl}, {q0.y, q1.y});
+                    const df::F2 drz = df::sub({bz, bzl}, {q0.z, q1.z});
+                    const df::F2 dd2 = df::add(df::add(df::sqr(drx), df::sqr(dry)), df::sqr(drz));
+                    const df::F2 sum = df::add({Ras, rows[r * kRowStride + 8]}, {Rbs, Rblo});
+                    const df::F2 gap2 = df::sub(df::sqr(sum), dd2);
+                    const float d2s = dd2.hi;
+                    const float inv_dn = rsqrtf(d2s);
+                    const float dist_s = d2s * inv_dn;
+                    const float ovl_s = __fdividef(gap2.hi, Ras + Rbs + dist_s);
+                    const float nx = drx.hi * inv_dn, ny = dry.hi * inv_dn, nz = drz.hi * inv_dn;
+                    if (gap2.hi > 0.0f || (gap2.hi == 0.0f && gap2.lo > 0.0f)) {
+                        contact = true;
+                        colbits |= 1u << r;
+                        const ContactIn in = gather_contact(s, A, B);
+                        // the kin/kout test compares |r|^2 with the previous step's,
+                        // both in FP64 from the FP64 positions with one formula
+                        const double d2_64 = fp64_d2(s, A, B);
+                        const ContactF o = contact_mixed(in, s.mat, sh, d2_64, nx, ny, nz, dist_s * L, ovl_s * L,
+                                                         Ras, Rbs);
+                        fx = o.fx; fy = o.fy; fz = o.fz;
+                        const float ima = s.f_inv_moi[A], imb = s.f_inv_moi[B];
+                        float* ta = tbuf + (size_t)A * s.npad + B;
+                        float* tb = tbuf + (size_t)B * s.npad + A;
+                        ta[0] = o.tax * ima; ta[plane] = o.tay * ima; ta[2 * plane] = o.taz * ima;
+                        tb[0] = o.tbx * imb; tb[plane] = o.tby * imb; tb[2 * plane] = o.tbz * imb;
+                        if (WRITE) {
+                            const double sum64 = s.R[A] + s.R[B];
+                            pe += pair_pe_fp64(s.mat, s.R[A], s.R[B], fma(sum64, sum64, -d2_64), d2_64, true, o.k);
+                        }
+                    } else {
+                        const float hn = fmaxf(-ovl_s, hmin_s);                 // :211-215
+                        const float f = c_vdw * vdw_shape(hn, Ras, Rbs);
+                        fx = f * nx; fy = f * ny; fz = f * nz;
+                    }
                 }
+                if (WRITE) {  // write steps only
+                    if (valid && !nearp) pe_far.add(vdw_bracket_far(T, Ras, Rbs));
+                    // near pairs out of contact: queued, evaluated 32 at a time
+                    const bool need = valid && nearp && !contact;
+                    const uint32_t m = __ballot_sync(0xffffffffu, need);
+                    if (m) {
+                        if (need) q[qn + __popc(m & ((1u << lane) - 1u))] = make_int2(X * kBlock + r, B);
+                        qn += __popc(m);
+                        __syncwarp();
+                        if (qn >= kBlock) flush_near(kBlock);
+                    }
+                }
+                if (!FULL && !valid) fx = fy = fz = 0.0f;
+                ax += fx; ay += fy; az += fz;
+                bsx += fx; bsy += fy; bsz += fz;
+                ax = __shfl_sync(0xffffffffu, ax, nxt);
+                ay = __shfl_sync(0xffffffffu, ay, nxt);
+                az = __shfl_sync(0xffffffffu, az, nxt);
             }
-            if (!valid) fx = fy = fz = 0.0f;
-            ax += fx; ay += fy; az += fz;
-            bsx += fx; bsy += fy; bsz += fz;
-            if (contact) colbits |= 1u << r;
-            ax = __shfl_sync(0xffffffffu, ax, nxt);
-            ay = __shfl_sync(0xffffffffu, ay, nxt);
-            az = __shfl_sync(0xffffffffu, az, nxt);
-        }
+        };
+        if (X != Y && (X + 1) * kBlock <= s.n)
+            sweep(std::true_type{});
+        else
+            sweep(std::false_type{});
         // lane l now holds row l's sum; its contact bits are the transpose of
         // the lanes' column bits
         uint32_t rowbits = 0;
@@ -213,6 +251,7 @@ __global__ void __launch_bounds__(32 * kPairWarps, 4) mixed_pair_kernel(const __
             s.cmask[ob] = colbits;
         }
         if (WRITE) {
+            if (qn > 0 && t + nwarps >= s.ntiles) flush_near(qn);  // the warp's last tile
             pe += -s.mat.Ha / 6 * (f2d_bits(pe_far.s) + f2d_bits(pe_far.c));
             for (int off = 16; off > 0; off >>= 1) pe += __shfl_xor_sync(0xffffffffu, pe, off);
             if (lane == 0) s.pe_tile[t] = pe;
@@ -221,18 +260,19 @@ __global__ void __launch_bounds__(32 * kPairWarps, 4) mixed_pair_kernel(const __
     }
 }
 
-constexpr int kFinSlices = 8;
+constexpr int kFinSlices = 16;
 
 // Per-sphere totals, then pass 3.  Block = 32 spheres (lanes) x kFinSlices
 // warps; warp w adds partner blocks [nb w / S, nb (w+1) / S) of its lane's
-// sphere: the force partials f_part[c][K][i] in compensated double-float sums
-// (coalesced loads along i), and the torque terms of contact partners (bits
-// of cmask[K][i], ascending) in FP64.  Warp 0 adds the slices in order and
-// integrates (ColliderSingleCore.cpp:263-267).
+// sphere: the force partials f_part[c][K][i] (coalesced loads along i) and
+// the torque terms of contact partners (bits of cmask[K][i], ascending), all
+// in compensated double-float sums.  Warp c < 3 then adds component c's
+// slices in order, still on the FP32 pipe, and integrates it in FP64
+// (ColliderSingleCore.cpp:263-267): a handful of FP64 instructions per warp,
+// which GB300 issues at one per 64 cycles or so.
 __global__ void __launch_bounds__(32 * kFinSlices) mixed_finish_kernel(const __grid_constant__ System s)
 {
-    __shared__ float fs[kFinSlices][6][kBlock];
-    __shared__ double ts[kFinSlices][3][kBlock];
+    __shared__ float fs[kFinSlices][12][kBlock];  // (s, c) of force x, y, z, then of torque x, y, z
     const int lane = threadIdx.x & 31;
     const int w = threadIdx.x >> 5;
     const int i = blockIdx.x * kBlock + lane;  // < npad
@@ -243,70 +283,69 @@ __global__ void __launch_bounds__(32 * kFinSlices) mixed_finish_kernel(const __g
     const float* p = s.f_part + i;
     const uint32_t* mk = s.cmask + i;
     const float* tb = reinterpret_cast<const float*>(s.torqbuf) + (size_t)i * s.npad;
-    df::Sum fx{0.0f, 0.0f}, fy{0.0f, 0.0f}, fz{0.0f, 0.0f};
-    double tx = 0, ty = 0, tz = 0;
+    df::Sum f[3] = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}};
+    df::Sum tq[3] = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}};
     auto torques = [&](uint32_t wd, int K) {
         while (wd) {
             const int j = K * kBlock + __ffs(wd) - 1;
             wd &= wd - 1;
-            tx += f2d_bits(tb[j]);
-            ty += f2d_bits(tb[j + plane]);
-            tz += f2d_bits(tb[j + 2 * plane]);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) tq[c].add(tb[j + c * plane]);
         }
     };
-    constexpr int U = 4;
+    constexpr int U = 8;  // loads in flight per array
     int K = K0;
     for (; K + U <= K1; K += U) {
-        float vx[U], vy[U], vz[U];
+        float v[3][U];
         uint32_t m[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             const size_t o = (size_t)(K + u) * s.npad;
-            vx[u] = __ldcs(p + o);
-            vy[u] = __ldcs(p + o + pplane);
-            vz[u] = __ldcs(p + o + 2 * pplane);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) v[c][u] = __ldcs(p + o + c * pplane);
             m[u] = __ldcs(mk + o);
         }
 #pragma unroll
         for (int u = 0; u < U; ++u) {
-            fx.add(vx[u]);
-            fy.add(vy[u]);
-            fz.add(vz[u]);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) f[c].add(v[c][u]);
             torques(m[u], K + u);
         }
     }
     for (; K < K1; ++K) {
         const size_t o = (size_t)K * s.npad;
-        fx.add(__ldcs(p + o));
-        fy.add(__ldcs(p + o + pplane));
-        fz.add(__ldcs(p + o + 2 * pplane));
+#pragma unroll
+        for (int c = 0; c < 3; ++c) f[c].add(__ldcs(p + o + c * pplane));
         torques(__ldcs(mk + o), K);
     }
-    fs[w][0][lane] = fx.s; fs[w][1][lane] = fx.c;
-    fs[w][2][lane] = fy.s; fs[w][3][lane] = fy.c;
-    fs[w][4][lane] = fz.s; fs[w][5][lane] = fz.c;
-    ts[w][0][lane] = tx; ts[w][1][lane] = ty; ts[w][2][lane] = tz;
-    __syncthreads();
-    if (w != 0 || i >= s.n) return;
-    const double dt = s.sc->dt;
-    bool bad = false;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        double acc = 0, aacc = 0;
-#pragma unroll
-        for (int ww = 0; ww < kFinSlices; ++ww) {
-            acc += f2d_bits(fs[ww][2 * c][lane]) + f2d_bits(fs[ww][2 * c + 1][lane]);
-            aacc += ts[ww][c][lane];
-        }
-        const double v = s.velh.c[c][i] + (.5 * acc) * dt;    // :265
-        const double wv = s.wh.c[c][i] + (.5 * aacc) * dt;   // :266
-        s.acc.c[c][i] = acc;
-        s.aacc.c[c][i] = aacc;
-        s.vel.c[c][i] = v;
-        s.w.c[c][i] = wv;
-        bad = bad || !isfinite(v) || !isfinite(wv) || !isfinite(s.pos.c[c][i]);
+        fs[w][2 * c][lane] = f[c].s;
+        fs[w][2 * c + 1][lane] = f[c].c;
+        fs[w][6 + 2 * c][lane] = tq[c].s;
+        fs[w][7 + 2 * c][lane] = tq[c].c;
     }
-    if (bad) atomicOr(s.status, 1u);
+    __syncthreads();
+    if (w >= 3 || i >= s.n) return;
+    const int c = w;
+    df::Sum F{0.0f, 0.0f}, Q{0.0f, 0.0f};
+#pragma unroll
+    for (int ww = 0; ww < kFinSlices; ++ww) {
+        F.add(fs[ww][2 * c][lane]);
+        F.add(fs[ww][2 * c + 1][lane]);
+        Q.add(fs[ww][6 + 2 * c][lane]);
+        Q.add(fs[ww][7 + 2 * c][lane]);
+    }
+    const double acc = f2d_bits(F.s) + f2d_bits(F.c);
+    const double aacc = f2d_bits(Q.s) + f2d_bits(Q.c);
+    const double dt = s.sc->dt;
+    const double v = s.velh.c[c][i] + (.5 * acc) * dt;    // :265
+    const double wv = s.wh.c[c][i] + (.5 * aacc) * dt;   // :266
+    s.acc.c[c][i] = acc;
+    s.aacc.c[c][i] = aacc;
+    s.vel.c[c][i] = v;
+    s.w.c[c][i] = wv;
+    if (!isfinite(v) || !isfinite(wv) || !isfinite(s.pos.c[c][i])) atomicOr(s.status, 1u);
 }
 
 }  // namespace
