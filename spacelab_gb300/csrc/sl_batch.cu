@@ -180,7 +180,9 @@ __global__ void batch_derive_kernel(const __grid_constant__ Batch b)
     b.rm[i] = recip_of(m);
     b.inv_moi[i] = 1.0 / moi;
     if (b.f_R) {
-        b.f_R[i] = d2f_bits(R, b.len_shift);
+        const float rh = d2f_bits(R, b.len_shift);
+        b.f_R[i] = rh;
+        b.f_Rlo[i] = d2f_bits(R - f2d_bits(rh) * ldexp(1.0, b.len_shift), b.len_shift);
         b.f_inv_m[i] = d2f_bits(1.0 / m, 0);
         b.f_inv_moi[i] = d2f_bits(1.0 / moi, 0);
     }

@@ -25,6 +25,14 @@ struct Batch {
     unsigned long long* rm;  // 64-bit fixed-point reciprocal significand of m (recip_sig)
     double* inv_moi;
     float *f_R, *f_inv_m, *f_inv_moi;  // mixed form (lengths scaled by 2^-len_shift)
+    // mixed form: the radii's double-float lo parts, and the positions as
+    // double-float hi (x, y, z) and lo (x, y, z), written by the drift
+    float *f_Rlo, *f_pos[6];
+    // mixed form: the order in which the pair pass assigns spheres to
+    // threads, perm[off + k] = off + the instance's k-th sphere in Z-order of
+    // its positions at upload, so that a warp's spheres are close together
+    // and few warps take the near-pair path for a given partner
+    const int* perm;
     int len_shift;
     Material mat;         // G, Ha, u_r, h_min shared; u_s per instance
     double* energy;       // [ninst][nrec][8]

@@ -101,6 +101,54 @@ int snapshot_copy(sl_batch* h, bool save)
 
 }  // namespace
 
+namespace {
+
+// Spreads the low 10 bits of x to every third bit (bits 0, 3, ..., 27).
+uint32_t spread3(uint32_t x)
+{
+    x &= 0x3ffu;
+    x = (x | (x << 16)) & 0x030000ffu;
+    x = (x | (x << 8)) & 0x0300f00fu;
+    x = (x | (x << 4)) & 0x030c30c3u;
+    x = (x | (x << 2)) & 0x09249249u;
+    return x;
+}
+
+// Per instance, its spheres' global indices sorted by the Z-order (Morton)
+// code of their positions quantised to 10 bits per axis over the instance's
+// bounding box; ties keep index order.
+std::vector<int> zorder_perm(const std::vector<int>& offsets, const std::vector<int>& counts, const double* pos)
+{
+    std::vector<int> perm;
+    perm.reserve(offsets.empty() ? 0 : offsets.back() + counts.back());
+    std::vector<std::pair<uint32_t, int>> key;
+    for (size_t inst = 0; inst < offsets.size(); ++inst) {
+        const int off = offsets[inst], n = counts[inst];
+        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+        for (int i = off; i < off + n; ++i)
+            for (int c = 0; c < 3; ++c) {
+                lo[c] = std::min(lo[c], pos[3 * (size_t)i + c]);
+                hi[c] = std::max(hi[c], pos[3 * (size_t)i + c]);
+            }
+        key.clear();
+        for (int i = off; i < off + n; ++i) {
+            uint32_t code = 0;
+            for (int c = 0; c < 3; ++c) {
+                const double ext = hi[c] - lo[c];
+                const double q = ext > 0 ? (pos[3 * (size_t)i + c] - lo[c]) / ext * 1023.0 : 0.0;
+                code |= spread3((uint32_t)std::min(1023.0, std::max(0.0, q))) << c;
+            }
+            key.emplace_back(code, i);
+        }
+        std::stable_sort(key.begin(), key.end(),
+                         [](const std::pair<uint32_t, int>& a, const std::pair<uint32_t, int>& c) { return a.first < c.first; });
+        for (const auto& k : key) perm.push_back(k.second);
+    }
+    return perm;
+}
+
+}  // namespace
+
 extern "C" {
 
 int sl_batch_create(int ninst, const int* counts, const sl_material* mat, int mode, int steps, int skip,
@@ -141,7 +189,7 @@ int sl_batch_create(int ninst, const int* counts, const sl_material* mat, int mo
     const size_t T = (size_t)total;
     size_t off = 0;
     auto take = [&](size_t bytes) { size_t o = off; off = align_up(off + bytes, 256); return o; };
-    size_t o_vec[8][3], o_sc[8], o_f[3];
+    size_t o_vec[8][3], o_sc[8], o_f[10];
     for (auto& v : o_vec)
         for (auto& c : v) c = take(T * sizeof(double));
     for (auto& s : o_sc) s = take(T * sizeof(double));
@@ -152,6 +200,7 @@ int sl_batch_create(int ninst, const int* counts, const sl_material* mat, int mo
     const size_t o_en = take((size_t)ninst * b.nrec * 8 * sizeof(double));
     const size_t o_st = take(ninst * sizeof(unsigned));
     const size_t o_snap = take(15 * T * sizeof(double));
+    const size_t o_perm = take(mode == SL_MODE_MIXED ? T * sizeof(int) : 0);
     h->arena_bytes = off;
     if (cudaMalloc(&h->arena, off) != cudaSuccess) {
         sl_batch_destroy(h);
@@ -169,6 +218,9 @@ int sl_batch_create(int ninst, const int* counts, const sl_material* mat, int mo
         b.f_R = reinterpret_cast<float*>(base + o_f[0]);
         b.f_inv_m = reinterpret_cast<float*>(base + o_f[1]);
         b.f_inv_moi = reinterpret_cast<float*>(base + o_f[2]);
+        b.f_Rlo = reinterpret_cast<float*>(base + o_f[3]);
+        for (int k = 0; k < 6; ++k) b.f_pos[k] = reinterpret_cast<float*>(base + o_f[4 + k]);
+        b.perm = reinterpret_cast<const int*>(base + o_perm);
     }
     int* order = reinterpret_cast<int*>(base + o_order);
     int* doff = reinterpret_cast<int*>(base + o_off);
@@ -250,6 +302,10 @@ int sl_batch_upload(sl_batch* h, const double* pos, const double* vel, const dou
     double* dpar = const_cast<double*>(b.dt);
     for (int k = 0; k < 4; ++k)
         SLB_CUDA(cudaMemcpy(dpar + (size_t)k * b.ninst, par[k], b.ninst * sizeof(double), cudaMemcpyHostToDevice));
+    if (b.perm) {
+        const std::vector<int> perm = zorder_perm(h->offsets, h->counts, pos);
+        SLB_CUDA(cudaMemcpy(const_cast<int*>(b.perm), perm.data(), T * sizeof(int), cudaMemcpyHostToDevice));
+    }
     SLB_CUDA(cudaMemset(b.status, 0, b.ninst * sizeof(unsigned)));
     sl::launch_batch_derive(b, h->stream);
     SLB_CUDA(cudaGetLastError());

@@ -41,6 +41,16 @@ __device__ __forceinline__ void drift(const Batch& b, int off, int n, double dt)
             b.prev.c[c][g] = p;
             b.pos.c[c][g] = p + vh * dt;                                   // :90
         }
+        if (b.f_pos[0]) {  // mixed form: scaled positions as double-float hi + lo
+            const double scale = ldexp(1.0, b.len_shift);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const double p = b.pos.c[c][g];
+                const float hi = d2f_bits(p, b.len_shift);
+                b.f_pos[c][g] = hi;
+                b.f_pos[3 + c][g] = d2f_bits(p - f2d_bits(hi) * scale, b.len_shift);
+            }
+        }
     }
 }
 

@@ -1,10 +1,12 @@
 // sl_batch_mixed.cu -- batched solver in the mixed-precision form: the same
 // persistent work-queue launch as sl_batch.cu, with the pair pass of the
-// mixed form: double-float (sl_df.cuh) displacement, |r|^2 and squared gap
-// from double-float splits of the scaled positions; FP32 forces and torques;
-// compensated FP32 per-sphere sums in ascending partner order, converted to
-// FP64; FP64 kin/kout test and write-step potential energy from the FP64
-// positions.  The non-contact pair path issues no FP64 instruction.
+// mixed form: far pairs entirely in FP32 (no square root), near pairs with
+// double-float (sl_df.cuh) displacement, |r|^2 and squared gap from the
+// double-float positions the drift writes; FP32 forces and torques; FP32
+// sums per j-tile joined in compensated per-sphere totals, converted to
+// FP64; FP64 kin/kout test and write-step potential energy of near pairs
+// from the FP64 positions (far pairs: the FP32 series of vdw_bracket_far).
+// The non-contact pair path issues no FP64 instruction.
 #include "sl_batch.h"
 #include "sl_batch_common.cuh"
 #include "sl_df.cuh"
@@ -19,16 +21,10 @@ using batch::kick;
 
 template <int TILE>
 struct JTileM {
-    float ph[3][TILE], pl[3][TILE];  // scaled position, double-float hi and lo
-    float Rs[TILE], Rlo[TILE];       // scaled radius, double-float hi and lo
+    float4 q0[TILE];  // scaled position hi x, y, z and scaled radius R
+    float4 q1[TILE];  // scaled position lo x, y, z and R^3
+    float Rlo[TILE];  // the radius's double-float lo part
 };
-
-// x * 2^-sh as a double-float (hi, lo)
-__device__ __forceinline__ df::F2 split_scaled(double x, int sh, double scale)
-{
-    const float hi = d2f_bits(x, sh);
-    return {hi, d2f_bits(x - f2d_bits(hi) * scale, sh)};
-}
 
 // |pos[gB] - pos[gA]|^2 in FP64, the previous-step formula of contact_mixed
 __device__ __forceinline__ double fp64_d2(const Batch& b, int gA, int gB)
@@ -39,6 +35,14 @@ __device__ __forceinline__ double fp64_d2(const Batch& b, int gA, int gB)
     return fma(rx, rx, fma(ry, ry, rz * rz));
 }
 
+// Thread i walks partners j through shared-memory j-tiles and adds the
+// force on i, F_ij, into a plain FP32 sum per tile, which joins i's
+// compensated total; acc[i] = total / m[i].  A far pair (|r| >= 2 (R_i + R_j))
+// takes the FP32 path of the all-pairs mixed kernel: vdW along
+// r = pos[j] - pos[i] without a square root, (c R_i^3 R_j^3) r / (S T)^2 with
+// S = |r|^2 - (R_i + R_j)^2 and T = |r|^2 - (R_i - R_j)^2; a near pair the
+// double-float geometry and, in contact, contact_mixed in the pair's own
+// (A, B) orientation (ColliderSingleCore.cpp:104-253).
 template <int TILE, bool WRITE>
 __device__ double pair_pass_mixed(const Batch& b, int off, int n, const Material& M, double kin, double kout,
                                   JTileM<TILE>& jt)
@@ -47,17 +51,17 @@ __device__ double pair_pass_mixed(const Batch& b, int off, int n, const Material
     const float L = ldexpf(1.0f, sh);
     const float hmin_s = (float)M.h_min / L;
     const float c_vdw = (float)(M.Ha / 6 * 64) / L;
-    const double scale = ldexp(1.0, sh);
     double pe = 0;
+    df::Sum pe_far{0.0f, 0.0f};  // far pairs' vdW brackets (write steps, i = A)
     for (int ibase = 0; ibase < n; ibase += blockDim.x) {
-        const int i = ibase + threadIdx.x;
-        const bool active = i < n;
-        const int gi = off + (active ? i : 0);
-        df::F2 pi[3];
-#pragma unroll
-        for (int c = 0; c < 3; ++c) pi[c] = split_scaled(b.pos.c[c][gi], sh, scale);
-        const df::F2 Ri = split_scaled(b.R[gi], sh, scale);
-        const float imi = b.f_inv_m[gi], imoii = b.f_inv_moi[gi];
+        const bool active = ibase + threadIdx.x < n;
+        const int gi = active ? b.perm[off + ibase + threadIdx.x] : off;  // Z-order: a warp's spheres are close
+        const int i = gi - off;
+        const float pih[3] = {b.f_pos[0][gi], b.f_pos[1][gi], b.f_pos[2][gi]};
+        const float pil[3] = {b.f_pos[3][gi], b.f_pos[4][gi], b.f_pos[5][gi]};
+        const float Ri = b.f_R[gi], Rilo = b.f_Rlo[gi];
+        const float cR3i = c_vdw * (Ri * Ri * Ri);
+        const float imoii = b.f_inv_moi[gi];
         df::Sum ax{0.0f, 0.0f}, ay{0.0f, 0.0f}, az{0.0f, 0.0f};
         double tx = 0, ty = 0, tz = 0;
         for (int jbase = 0; jbase < n; jbase += TILE) {
@@ -65,84 +69,103 @@ __device__ double pair_pass_mixed(const Batch& b, int off, int n, const Material
                 const int j = jbase + t;
                 if (j < n) {
                     const int g = off + j;
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) {
-                        const df::F2 v = split_scaled(b.pos.c[c][g], sh, scale);
-                        jt.ph[c][t] = v.hi;
-                        jt.pl[c][t] = v.lo;
-                    }
-                    const df::F2 r = split_scaled(b.R[g], sh, scale);
-                    jt.Rs[t] = r.hi;
-                    jt.Rlo[t] = r.lo;
+                    const float r = b.f_R[g];
+                    jt.q0[t] = make_float4(b.f_pos[0][g], b.f_pos[1][g], b.f_pos[2][g], r);
+                    jt.q1[t] = make_float4(b.f_pos[3][g], b.f_pos[4][g], b.f_pos[5][g], r * r * r);
+                    jt.Rlo[t] = b.f_Rlo[g];
                 }
             }
             __syncthreads();
             if (active) {
                 const int jend = min(TILE, n - jbase);
+                float sx = 0, sy = 0, sz = 0;  // this tile's forces on i
                 for (int t = 0; t < jend; ++t) {
                     const int j = jbase + t;
-                    if (j == i) continue;
+                    const bool valid = j != i;
+                    const float4 q0 = jt.q0[t], q1 = jt.q1[t];
+                    const float Rj = q0.w;
+                    const float rx = (q0.x - pih[0]) + (q1.x - pil[0]);
+                    const float ry = (q0.y - pih[1]) + (q1.y - pil[1]);
+                    const float rz = (q0.z - pih[2]) + (q1.z - pil[2]);
+                    const float d2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
+                    const float sumR = Ri + Rj, difR = Ri - Rj;
+                    const float sum2 = sumR * sumR;
+                    const float S = d2 - sum2;
+                    const float T = fmaf(-difR, difR, d2);
+                    const float P = S * T;
+                    const float fr = (cR3i * q1.w) * rcp_approx(P * P);
+                    float fx = fr * rx, fy = fr * ry, fz = fr * rz;
+                    const bool nearp = d2 < 4.0f * sum2;
                     const bool iA = i > j;
-                    // r = pos[B] - pos[A] in double-float; the sign flips with the orientation
-                    df::F2 r3[3];
+                    if (valid && nearp) {
+                        // r = pos[B] - pos[A] in double-float; the sign flips with the orientation
+                        const df::F2 pj[3] = {{q0.x, q1.x}, {q0.y, q1.y}, {q0.z, q1.z}};
+                        df::F2 r3[3];
 #pragma unroll
-                    for (int c = 0; c < 3; ++c) {
-                        const df::F2 pj{jt.ph[c][t], jt.pl[c][t]};
-                        r3[c] = iA ? df::sub(pj, pi[c]) : df::sub(pi[c], pj);
-                    }
-                    const df::F2 d2 = df::add(df::add(df::sqr(r3[0]), df::sqr(r3[1])), df::sqr(r3[2]));
-                    const df::F2 sum = df::add(Ri, {jt.Rs[t], jt.Rlo[t]});
-                    const df::F2 gap2 = df::sub(df::sqr(sum), d2);
-                    const float Ras = iA ? Ri.hi : jt.Rs[t], Rbs = iA ? jt.Rs[t] : Ri.hi;
-                    const float rxs = r3[0].hi, rys = r3[1].hi, rzs = r3[2].hi;
-                    const float d2s = d2.hi;
-                    const float inv_d = rsqrtf(d2s);
-                    const float dist_s = d2s * inv_d;
-                    const float ovl_s = __fdividef(gap2.hi, Ras + Rbs + dist_s);
-                    const float nx = rxs * inv_d, ny = rys * inv_d, nz = rzs * inv_d;
-                    float fx, fy, fz;
-                    const int gA = off + (iA ? i : j), gB = off + (iA ? j : i);
-                    if (gap2.hi > 0.0f || (gap2.hi == 0.0f && gap2.lo > 0.0f)) {
-                        ContactIn in;
                         for (int c = 0; c < 3; ++c) {
-                            in.prevA[c] = b.prev.c[c][gA]; in.prevB[c] = b.prev.c[c][gB];
-                            in.wA[c] = b.w.c[c][gA]; in.wB[c] = b.w.c[c][gB];
-                            in.vA[c] = b.vel.c[c][gA]; in.vB[c] = b.vel.c[c][gB];
+                            const df::F2 pi{pih[c], pil[c]};
+                            r3[c] = iA ? df::sub(pj[c], pi) : df::sub(pi, pj[c]);
                         }
-                        in.mA = b.m[gA]; in.mB = b.m[gB]; in.kin = kin; in.kout = kout;
-                        // kin/kout: |r|^2 against the previous step's, both FP64 by one formula
-                        const double d2_64 = fp64_d2(b, gA, gB);
-                        const ContactF o = contact_mixed(in, M, sh, d2_64, nx, ny, nz, dist_s * L, ovl_s * L, Ras,
-                                                         Rbs);
-                        fx = o.fx; fy = o.fy; fz = o.fz;
-                        const float qx = iA ? o.tax : o.tbx, qy = iA ? o.tay : o.tby, qz = iA ? o.taz : o.tbz;
-                        tx += f2d_bits(qx * imoii); ty += f2d_bits(qy * imoii); tz += f2d_bits(qz * imoii);
-                        if (WRITE && iA) {
-                            const double sum64 = b.R[gA] + b.R[gB];
-                            pe += pair_pe_fp64(M, b.R[gA], b.R[gB], fma(sum64, sum64, -d2_64), d2_64, true, o.k);
+                        const df::F2 dd2 = df::add(df::add(df::sqr(r3[0]), df::sqr(r3[1])), df::sqr(r3[2]));
+                        const df::F2 sum = df::add({Ri, Rilo}, {Rj, jt.Rlo[t]});
+                        const df::F2 gap2 = df::sub(df::sqr(sum), dd2);
+                        const float Ras = iA ? Ri : Rj, Rbs = iA ? Rj : Ri;
+                        const float d2s = dd2.hi;
+                        const float inv_d = rsqrtf(d2s);
+                        const float dist_s = d2s * inv_d;
+                        const float ovl_s = __fdividef(gap2.hi, Ras + Rbs + dist_s);
+                        const float nx = r3[0].hi * inv_d, ny = r3[1].hi * inv_d, nz = r3[2].hi * inv_d;
+                        float Fx, Fy, Fz;  // force on A
+                        const int gA = off + (iA ? i : j), gB = off + (iA ? j : i);
+                        if (gap2.hi > 0.0f || (gap2.hi == 0.0f && gap2.lo > 0.0f)) {
+                            ContactIn in;
+                            for (int c = 0; c < 3; ++c) {
+                                in.prevA[c] = b.prev.c[c][gA]; in.prevB[c] = b.prev.c[c][gB];
+                                in.wA[c] = b.w.c[c][gA]; in.wB[c] = b.w.c[c][gB];
+                                in.vA[c] = b.vel.c[c][gA]; in.vB[c] = b.vel.c[c][gB];
+                            }
+                            in.mA = b.m[gA]; in.mB = b.m[gB]; in.kin = kin; in.kout = kout;
+                            // kin/kout: |r|^2 against the previous step's, both FP64 by one formula
+                            const double d2_64 = fp64_d2(b, gA, gB);
+                            const ContactF o = contact_mixed(in, M, sh, d2_64, nx, ny, nz, dist_s * L, ovl_s * L, Ras,
+                                                             Rbs);
+                            Fx = o.fx; Fy = o.fy; Fz = o.fz;
+                            const float qx = iA ? o.tax : o.tbx, qy = iA ? o.tay : o.tby, qz = iA ? o.taz : o.tbz;
+                            tx += f2d_bits(qx * imoii); ty += f2d_bits(qy * imoii); tz += f2d_bits(qz * imoii);
+                            if (WRITE && iA) {
+                                const double sum64 = b.R[gA] + b.R[gB];
+                                pe += pair_pe_fp64(M, b.R[gA], b.R[gB], fma(sum64, sum64, -d2_64), d2_64, true, o.k);
+                            }
+                        } else {
+                            const float h = fmaxf(-ovl_s, hmin_s);
+                            const float f = c_vdw * vdw_shape(h, Ras, Rbs);
+                            Fx = f * nx; Fy = f * ny; Fz = f * nz;
+                            if (WRITE && iA) {
+                                const double d2_64 = fp64_d2(b, gA, gB), sum64 = b.R[gA] + b.R[gB];
+                                pe += pair_pe_fp64(M, b.R[gA], b.R[gB], fma(sum64, sum64, -d2_64), d2_64, false,
+                                                   0.0);
+                            }
                         }
-                    } else {
-                        const float h = fmaxf(-ovl_s, hmin_s);
-                        const float f = c_vdw * vdw_shape(h, Ras, Rbs);
-                        fx = f * nx; fy = f * ny; fz = f * nz;
-                        if (WRITE && iA) {
-                            const double d2_64 = fp64_d2(b, gA, gB), sum64 = b.R[gA] + b.R[gB];
-                            pe += pair_pe_fp64(M, b.R[gA], b.R[gB], fma(sum64, sum64, -d2_64), d2_64, false, 0.0);
-                        }
+                        // acc[A] += F/m[A]; acc[B] -= F/m[B]
+                        fx = iA ? Fx : -Fx; fy = iA ? Fy : -Fy; fz = iA ? Fz : -Fz;
                     }
-                    const float s = iA ? imi : -imi;  // acc[A] += F/m[A]; acc[B] -= F/m[B]
-                    ax.add(fx * s); ay.add(fy * s); az.add(fz * s);
+                    if (WRITE && valid && iA && !nearp) pe_far.add(vdw_bracket_far(T, Ri, Rj));
+                    if (!valid) fx = fy = fz = 0.0f;
+                    sx += fx; sy += fy; sz += fz;
                 }
+                ax.add(sx); ay.add(sy); az.add(sz);
             }
             __syncthreads();
         }
         if (active) {
-            b.acc.c[0][gi] = f2d_bits(ax.s) + f2d_bits(ax.c);
-            b.acc.c[1][gi] = f2d_bits(ay.s) + f2d_bits(ay.c);
-            b.acc.c[2][gi] = f2d_bits(az.s) + f2d_bits(az.c);
+            const double imi = f2d_bits(b.f_inv_m[gi]);
+            b.acc.c[0][gi] = (f2d_bits(ax.s) + f2d_bits(ax.c)) * imi;
+            b.acc.c[1][gi] = (f2d_bits(ay.s) + f2d_bits(ay.c)) * imi;
+            b.acc.c[2][gi] = (f2d_bits(az.s) + f2d_bits(az.c)) * imi;
             b.aacc.c[0][gi] = tx; b.aacc.c[1][gi] = ty; b.aacc.c[2][gi] = tz;
         }
     }
+    if (WRITE) pe += -M.Ha / 6 * (f2d_bits(pe_far.s) + f2d_bits(pe_far.c));
     return pe;
 }
 
