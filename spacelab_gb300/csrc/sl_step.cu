@@ -35,30 +35,30 @@
 namespace sl {
 
 // ---------------------------------------------------------------- pass 1 --
-__global__ void __launch_bounds__(256) drift_kernel(const __grid_constant__ System s)
+// One thread per (component, sphere), in small blocks: the few FP64
+// operations per thread then spread over every SM sub-partition's FP64 unit
+// (one warp instruction per ~64 cycles each) instead of queueing on a few.
+constexpr int kDriftThreads = 64;
+
+__global__ void __launch_bounds__(kDriftThreads) drift_kernel(const __grid_constant__ System s)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= s.n) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 3 * s.n) return;
+    const int c = t / s.n;
+    const int i = t - c * s.n;
     const double dt = s.sc->dt;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        const double vh = s.vel.c[c][i] + (.5 * s.acc.c[c][i]) * dt;   // :84
-        const double whc = s.w.c[c][i] + (.5 * s.aacc.c[c][i]) * dt;   // :87
-        const double p = s.pos.c[c][i];
-        s.velh.c[c][i] = vh;
-        s.wh.c[c][i] = whc;
-        s.prev.c[c][i] = p;            // positions the pair distances of
-        s.pos.c[c][i] = p + vh * dt;   // the previous step were taken at; :90
-    }
-    if (s.f_pos[0]) {  // mixed form: scaled positions as double-float hi + lo
-        const double scale = ldexp(1.0, s.len_shift);
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            const double p = s.pos.c[c][i];
-            const float hi = d2f_bits(p, s.len_shift);
-            s.f_pos[c][i] = hi;
-            s.f_pos[3 + c][i] = d2f_bits(p - f2d_bits(hi) * scale, s.len_shift);
-        }
+    const double vh = s.vel.c[c][i] + (.5 * s.acc.c[c][i]) * dt;   // :84
+    const double whc = s.w.c[c][i] + (.5 * s.aacc.c[c][i]) * dt;   // :87
+    const double p = s.pos.c[c][i];
+    const double pn = p + vh * dt;                                  // :90
+    s.velh.c[c][i] = vh;
+    s.wh.c[c][i] = whc;
+    s.prev.c[c][i] = p;  // positions the pair distances of the previous step were taken at
+    s.pos.c[c][i] = pn;
+    if (s.f_pos[0]) {  // mixed form: scaled position as double-float hi + lo
+        const float hi = d2f_bits(pn, s.len_shift);
+        s.f_pos[c][i] = hi;
+        s.f_pos[3 + c][i] = d2f_bits(pn - f2d_bits(hi) * ldexp(1.0, s.len_shift), s.len_shift);
     }
 }
 
@@ -455,7 +455,7 @@ void launch_stage_out(const System& s, double* stage, Vec3Soa* const arr[6], uns
 
 void launch_drift(const System& s, cudaStream_t st)
 {
-    drift_kernel<<<(s.n + 255) / 256, 256, 0, st>>>(s);
+    drift_kernel<<<(3 * s.n + kDriftThreads - 1) / kDriftThreads, kDriftThreads, 0, st>>>(s);
 }
 
 void launch_energy(const System& s, cudaStream_t st)

@@ -52,6 +52,7 @@ namespace {
 //   [8] the radius's lo part, [9] 1/m.
 constexpr int kRowStride = 12;
 constexpr int kPairWarps = 4;
+constexpr int kPairCtasPerSm = 5;  // resident CTAs per SM (the launch bounds' minimum)
 
 // |pos[B] - pos[A]|^2 in FP64, the formula of the previous-step distance in
 // contact_mixed (rare paths: the contact test, write-step energies).
@@ -70,7 +71,7 @@ __device__ __forceinline__ double fp64_d2(const System& s, int A, int B)
 // f_part[c][X][i] with both; contact bits to cmask[K][i]; torques of contacts
 // to the float view of torqbuf, [A][B] and [B][A].
 template <bool WRITE>
-__global__ void __launch_bounds__(32 * kPairWarps, 4) mixed_pair_kernel(const __grid_constant__ System s)
+__global__ void __launch_bounds__(32 * kPairWarps, kPairCtasPerSm) mixed_pair_kernel(const __grid_constant__ System s)
 {
     __shared__ __align__(16) float rows_all[kPairWarps][kBlock * kRowStride];
     const int lane = threadIdx.x & 31;
@@ -355,7 +356,7 @@ void launch_step_mixed(const System& s, bool write, int num_sms, cudaStream_t st
     launch_drift(s, st);
     if (tm) cudaEventRecord(tm->ev[0], st);
     long long want = (s.ntiles + kPairWarps - 1) / kPairWarps;
-    long long cap = (long long)num_sms * 4;  // 4 CTAs (16 warps) per SM
+    long long cap = (long long)num_sms * kPairCtasPerSm;  // one wave of persistent warps
     const int pb = (int)(want < cap ? want : cap);
     if (write)
         mixed_pair_kernel<true><<<pb, 32 * kPairWarps, 0, st>>>(s);
