@@ -33,6 +33,7 @@ struct Batch {
     // its positions at upload, so that a warp's spheres are close together
     // and few warps take the near-pair path for a given partner
     const int* perm;
+    float far_sq, series_sq;  // far-pair thresholds (far_thresholds in sl_pair_mixed.cuh)
     int len_shift;
     Material mat;         // G, Ha, u_r, h_min shared; u_s per instance
     double* energy;       // [ninst][nrec][8]

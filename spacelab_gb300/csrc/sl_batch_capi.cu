@@ -5,6 +5,7 @@
 #include "../../include/spacelab_batch.h"
 #include "../../include/spacelab_gpu.h"
 #include "sl_batch.h"
+#include "sl_pair_mixed.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -283,6 +284,9 @@ int sl_batch_upload(sl_batch* h, const double* pos, const double* vel, const dou
     int ex = 0;
     std::frexp(rmax, &ex);
     b.len_shift = ex - 1;
+    double rmin = R[0];
+    for (size_t i = 0; i < T; ++i) rmin = std::min(rmin, R[i]);
+    sl::far_thresholds(b.mat.h_min, rmin, b.far_sq, b.series_sq);
     std::vector<double> tmp(T);
     const double* v3[3] = {pos, vel, w};
     sl::Vec3Soa* dv[3] = {&b.pos, &b.vel, &b.w};

@@ -37,8 +37,9 @@ __device__ __forceinline__ double fp64_d2(const Batch& b, int gA, int gB)
 
 // Thread i walks partners j through shared-memory j-tiles and adds the
 // force on i, F_ij, into a plain FP32 sum per tile, which joins i's
-// compensated total; acc[i] = total / m[i].  A far pair (|r| >= 2 (R_i + R_j))
-// takes the FP32 path of the all-pairs mixed kernel: vdW along
+// compensated total; acc[i] = total / m[i].  A far pair
+// (|r| >= 1.25 (R_i + R_j) or more, far_sq) takes the FP32 path of the all-pairs mixed
+// kernel: vdW along
 // r = pos[j] - pos[i] without a square root, (c R_i^3 R_j^3) r / (S T)^2 with
 // S = |r|^2 - (R_i + R_j)^2 and T = |r|^2 - (R_i - R_j)^2; a near pair the
 // double-float geometry and, in contact, contact_mixed in the pair's own
@@ -95,9 +96,9 @@ __device__ double pair_pass_mixed(const Batch& b, int off, int n, const Material
                     const float P = S * T;
                     const float fr = (cR3i * q1.w) * rcp_approx(P * P);
                     float fx = fr * rx, fy = fr * ry, fz = fr * rz;
-                    const bool nearp = d2 < 4.0f * sum2;
+                    const bool nearp = d2 < b.series_sq * sum2;  // outside the far-pair potential series' range
                     const bool iA = i > j;
-                    if (valid && nearp) {
+                    if (valid && d2 < b.far_sq * sum2) {  // close pair
                         // r = pos[B] - pos[A] in double-float; the sign flips with the orientation
                         const df::F2 pj[3] = {{q0.x, q1.x}, {q0.y, q1.y}, {q0.z, q1.z}};
                         df::F2 r3[3];
@@ -149,7 +150,15 @@ __device__ double pair_pass_mixed(const Batch& b, int off, int n, const Material
                         // acc[A] += F/m[A]; acc[B] -= F/m[B]
                         fx = iA ? Fx : -Fx; fy = iA ? Fy : -Fy; fz = iA ? Fz : -Fz;
                     }
-                    if (WRITE && valid && iA && !nearp) pe_far.add(vdw_bracket_far(T, Ri, Rj));
+                    if (WRITE && valid && iA && !(d2 < b.far_sq * sum2)) {
+                        if (!nearp) {
+                            pe_far.add(vdw_bracket_far(T, Ri, Rj));
+                        } else {  // outside the series' range: FP64, as the close pairs
+                            const double d2_64 = fp64_d2(b, off + i, off + j), sum64 = b.R[off + i] + b.R[off + j];
+                            pe += pair_pe_fp64(M, b.R[off + i], b.R[off + j], fma(sum64, sum64, -d2_64), d2_64, false,
+                                               0.0);
+                        }
+                    }
                     if (!valid) fx = fy = fz = 0.0f;
                     sx += fx; sy += fy; sz += fz;
                 }

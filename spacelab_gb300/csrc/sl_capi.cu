@@ -9,6 +9,7 @@
 #include "../../include/spacelab_gpu.h"
 #include "sl_device.cuh"
 #include "sl_kernels.h"
+#include "sl_pair_mixed.cuh"
 
 #include <cmath>
 #include <cstdio>
@@ -228,6 +229,7 @@ int sl_create(int n, const sl_material* mat, int mode, sl_handle** out)
     const size_t o_red = take(sl::kRedBlocks * 8 * sizeof(double));
     const size_t o_en = take(8 * sizeof(double));
     const size_t o_st = take(sizeof(unsigned int));
+    const size_t o_tc = take(mixed ? sizeof(int) : 0);
     const size_t o_scl = take(sizeof(sl::Scalars));
     const size_t o_dstage = take(6 * 3 * np * sizeof(double));
     h->arena_bytes = off;
@@ -258,6 +260,7 @@ int sl_create(int n, const sl_material* mat, int mode, sl_handle** out)
     s.red = reinterpret_cast<double*>(base + o_red);
     s.energy = reinterpret_cast<double*>(base + o_en);
     s.status = reinterpret_cast<unsigned int*>(base + o_st);
+    if (mixed) s.tile_counter = reinterpret_cast<int*>(base + o_tc);
     h->d_sc = reinterpret_cast<sl::Scalars*>(base + o_scl);
     h->d_stage = reinterpret_cast<double*>(base + o_dstage);
     s.sc = h->d_sc;
@@ -317,11 +320,15 @@ int sl_upload(sl_handle* h, const double* pos, const double* vel, const double* 
     }
     if (int r = sl_upload_resume(h, pos, vel, w, nullptr, nullptr, nullptr)) return r;
     // length scale of the mixed form: 2^len_shift within a factor 2 of max R
-    double rmax = 0;
-    for (int i = 0; i < n; ++i) rmax = R[i] > rmax ? R[i] : rmax;
+    double rmax = 0, rmin = R[0];
+    for (int i = 0; i < n; ++i) {
+        rmax = R[i] > rmax ? R[i] : rmax;
+        rmin = R[i] < rmin ? R[i] : rmin;
+    }
     int ex = 0;
     std::frexp(rmax, &ex);
     h->sys.len_shift = ex - 1;
+    sl::far_thresholds(h->sys.mat.h_min, rmin, h->sys.far_sq, h->sys.series_sq);
     // padded spheres get R = m = moi = 1 (they are never paired)
     const double* src[3] = {R, m, moi};
     double* dst[3] = {h->sys.R, h->sys.m, h->sys.moi};

@@ -68,7 +68,12 @@ struct System {
     // (c, K, i) is component c of sphere i's acceleration terms from the
     // partners in 32-sphere block K
     float* f_part;
+    // mixed form: the pair kernel's tile counter (zeroed by the drift kernel)
+    int* tile_counter;
     int len_shift;
+    // mixed form: squared separation factors of the far-pair force and
+    // potential paths (far_thresholds in sl_pair_mixed.cuh)
+    float far_sq, series_sq;
 };
 
 // Operands of a pair's contact branch beyond positions and radii (the

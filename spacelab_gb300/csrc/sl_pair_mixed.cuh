@@ -21,6 +21,23 @@ __device__ __forceinline__ float vdw_shape(float h, float Ra, float Rb)
     return __fdividef(r3 * (h + sum), (S * S) * (T * T));
 }
 
+// Pairs with |r|^2 >= far_sq (R_A + R_B)^2 take the FP32 vdW path without a
+// square root.  far = max(1.25, 1 + h_min / (2 R_min)): their gap
+// h = |r| - R_A - R_B is then at least (R_A + R_B) / 4 and above the clamp
+// h_min, so S = |r|^2 - (R_A + R_B)^2 = h (h + 2 (R_A + R_B)) keeps all but
+// ~1.5 bits of |r|^2's precision, and the force comes out within ~2e-6 of the
+// FP64 formula (measured over separations 1.25-4 radii sums, split positions
+// up to 60 radii from the origin).  Closer pairs -- contacts and small gaps --
+// take the double-float geometry.  The far-pair potential series needs
+// |r| >= 2 (R_A + R_B) as well: series_sq = max(4, far_sq).
+inline void far_thresholds(double h_min, double r_min, float& far_sq, float& series_sq)
+{
+    double far = 1.0 + h_min / (2.0 * r_min);
+    if (far < 1.25) far = 1.25;
+    far_sq = (float)(far * far);
+    series_sq = far_sq > 4.0f ? far_sq : 4.0f;
+}
+
 // Approximate FP32 reciprocal (one MUFU instruction, relative error below
 // 2^-22; subnormal inputs and results flush to zero).
 __device__ __forceinline__ float rcp_approx(float x)

@@ -7,7 +7,7 @@
 //     energy of near pairs and the energy totals (far pairs' vdW potential
 //     comes from a cancellation-free series in FP32, vdw_bracket_far);
 //   * double-float (hi + lo FP32 pairs, ~48 significant bits, sl_df.cuh):
-//     for pairs closer than twice the sum of their radii, the subtraction
+//     for pairs closer than 1.25 times the sum of their radii, the subtraction
 //     r = pos[B] - pos[A] from double-float copies of the scaled positions,
 //     |r|^2 and the squared gap g = (R_A + R_B)^2 - |r|^2, from which the
 //     overlap is taken as g / (R_A + R_B + |r|) -- no cancellation in
@@ -16,10 +16,10 @@
 // Everything else -- distances, the vdW coefficient, elastic, gravity,
 // sliding and rolling friction, torques -- is FP32 on lengths scaled by
 // 2^-len_shift (about one radius), which keeps R^6 / (S^2 T^2) far from
-// FP32's range limits.  A pair at least twice its radii sum apart has a gap
-// h >= R_A + R_B, so FP32 geometry (r from the hi and lo parts) keeps
-// |r|^2 - (R_A +- R_B)^2 to a few ulp, and its vdW force needs no square
-// root: such pairs, nearly all of them, take a short FP32-only path.  No pair issues an FP64 instruction outside the contact
+// FP32's range limits.  A pair at least 1.25 times its radii sum apart has a
+// gap h >= (R_A + R_B) / 4, so FP32 geometry (r from the hi and lo parts)
+// keeps |r|^2 - (R_A +- R_B)^2 to a few ulp, and its vdW force needs no
+// square root: such pairs, nearly all of them, take a short FP32-only path.  No pair issues an FP64 instruction outside the contact
 // branch and write steps: GB300's FP32 pipe is ~72x its FP64 pipe.
 //
 // Accumulation: the pair terms never reach memory.  A warp evaluates a
@@ -107,7 +107,13 @@ __global__ void __launch_bounds__(32 * kPairWarps, kPairCtasPerSm) mixed_pair_ke
         qn = left;
     };
 
-    for (long long t = (long long)blockIdx.x * kPairWarps + wib; t < s.ntiles; t += nwarps) {
+    // Tiles: a first round in warp order, then, on plain steps, whichever
+    // warp is free takes the next tile from a counter that the drift kernel
+    // zeroes (the last round of a static stride leaves SMs idle); write
+    // steps keep the static stride, so that their near-pair queues, and so
+    // the potential energy's rounding, repeat run to run.
+    long long t = (long long)blockIdx.x * kPairWarps + wib;
+    for (; t < s.ntiles;) {
         int X, Y;
         tile_coords(t, X, Y);
         {
@@ -143,12 +149,12 @@ __global__ void __launch_bounds__(32 * kPairWarps, kPairCtasPerSm) mixed_pair_ke
                 const float4 q0 = *reinterpret_cast<const float4*>(rows + r * kRowStride);
                 const float4 q1 = *reinterpret_cast<const float4*>(rows + r * kRowStride + 4);
                 const float Ras = q0.w;
-                // far pairs, |r| >= 2 (R_A + R_B), in FP32 (scaled lengths): the
-                // gap h = |r| - R_A - R_B is then at least R_A + R_B, so the vdW
-                // force (:205-226) Ra^3 Rb^3 (h + Ra + Rb) / (S^2 T^2) along r/|r|
-                // needs no square root: h + Ra + Rb = |r|, S = h (h + 2(Ra + Rb))
-                // = |r|^2 - (Ra + Rb)^2 and T = S + 4 Ra Rb = |r|^2 - (Ra - Rb)^2,
-                // neither cancelling by more than a quarter
+                // pairs out of contact with h = |r| - R_A - R_B above the clamp
+                // h_min, in FP32 (scaled lengths): the vdW force (:205-226)
+                // Ra^3 Rb^3 (h + Ra + Rb) / (S^2 T^2) along r/|r| needs no square
+                // root: h + Ra + Rb = |r|, S = h (h + 2(Ra + Rb)) = |r|^2 - (Ra + Rb)^2
+                // and T = S + 4 Ra Rb = |r|^2 - (Ra - Rb)^2; used for |r| >= 1.25
+                // (Ra + Rb) or more, where S cancels little (far_sq)
                 const float rx = (bx - q0.x) + (bxl - q1.x);
                 const float ry = (by - q0.y) + (byl - q1.y);
                 const float rz = (bz - q0.z) + (bzl - q1.z);
@@ -161,9 +167,9 @@ __global__ void __launch_bounds__(32 * kPairWarps, kPairCtasPerSm) mixed_pair_ke
                 const float fr = (q1.w * Rb3) * rcp_approx(P * P);  // |F| / |r|
                 float fx = fr * rx, fy = fr * ry, fz = fr * rz;
                 bool contact = false;
-                const bool nearp = d2 < 4.0f * sum2;
-                if (valid && nearp) {
-                    // near pair: double-float (~48 bits, FP32 pipe) subtraction,
+                const bool nearp = d2 < s.series_sq * sum2;  // outside the far-pair potential series' range
+                if (valid && d2 < s.far_sq * sum2) {
+                    // close pair: double-float (~48 bits, FP32 pipe) subtraction,
                     // |r|^2 and squared gap g = (R_A + R_B)^2 - |r|^2
                     const int A = X * kBlock + r;
                     const df::F2 drx = df::sub({bx, bxl}, {q0.x, q1.x});
@@ -258,6 +264,13 @@ __global__ void __launch_bounds__(32 * kPairWarps, kPairCtasPerSm) mixed_pair_ke
             if (lane == 0) s.pe_tile[t] = pe;
         }
         __syncwarp();
+        if (WRITE) {
+            t += nwarps;
+        } else {
+            int k = 0;
+            if (lane == 0) k = atomicAdd(s.tile_counter, 1);
+            t = nwarps + __shfl_sync(0xffffffffu, k, 0);
+        }
     }
 }
 
