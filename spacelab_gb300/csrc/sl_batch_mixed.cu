@@ -78,9 +78,65 @@ __device__ double pair_pass_mixed(const Batch& b, int off, int n, const Material
             }
             __syncthreads();
             if (active) {
-                const int jend = min(TILE, n - jbase);
-                float sx = 0, sy = 0, sz = 0;  // this tile's forces on i
-                for (int t = 0; t < jend; ++t) {
+                // close pair j = jbase + t: double-float geometry, contact or
+                // clamped vdW in the pair's (A, B) orientation; the force on i
+                auto close_pair = [&](int t, float& fx, float& fy, float& fz) {
+                    const int j = jbase + t;
+                    const bool iA = i > j;
+                    const float4 q0 = jt.q0[t], q1 = jt.q1[t];
+                    const float Rj = q0.w;
+                    // r = pos[B] - pos[A] in double-float; the sign flips with the orientation
+                    const df::F2 pj[3] = {{q0.x, q1.x}, {q0.y, q1.y}, {q0.z, q1.z}};
+                    df::F2 r3[3];
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        const df::F2 pi{pih[c], pil[c]};
+                        r3[c] = iA ? df::sub(pj[c], pi) : df::sub(pi, pj[c]);
+                    }
+                    const df::F2 dd2 = df::add(df::add(df::sqr(r3[0]), df::sqr(r3[1])), df::sqr(r3[2]));
+                    const df::F2 sum = df::add({Ri, Rilo}, {Rj, jt.Rlo[t]});
+                    const df::F2 gap2 = df::sub(df::sqr(sum), dd2);
+                    const float Ras = iA ? Ri : Rj, Rbs = iA ? Rj : Ri;
+                    const float d2s = dd2.hi;
+                    const float inv_d = rsqrtf(d2s);
+                    const float dist_s = d2s * inv_d;
+                    const float ovl_s = __fdividef(gap2.hi, Ras + Rbs + dist_s);
+                    const float nx = r3[0].hi * inv_d, ny = r3[1].hi * inv_d, nz = r3[2].hi * inv_d;
+                    float Fx, Fy, Fz;  // force on A
+                    const int gA = off + (iA ? i : j), gB = off + (iA ? j : i);
+                    if (gap2.hi > 0.0f || (gap2.hi == 0.0f && gap2.lo > 0.0f)) {
+                        ContactIn in;
+                        for (int c = 0; c < 3; ++c) {
+                            in.prevA[c] = b.prev.c[c][gA]; in.prevB[c] = b.prev.c[c][gB];
+                            in.wA[c] = b.w.c[c][gA]; in.wB[c] = b.w.c[c][gB];
+                            in.vA[c] = b.vel.c[c][gA]; in.vB[c] = b.vel.c[c][gB];
+                        }
+                        in.mA = b.m[gA]; in.mB = b.m[gB]; in.kin = kin; in.kout = kout;
+                        // kin/kout: |r|^2 against the previous step's, both FP64 by one formula
+                        const double d2_64 = fp64_d2(b, gA, gB);
+                        const ContactF o = contact_mixed(in, M, sh, d2_64, nx, ny, nz, dist_s * L, ovl_s * L, Ras, Rbs);
+                        Fx = o.fx; Fy = o.fy; Fz = o.fz;
+                        const float qx = iA ? o.tax : o.tbx, qy = iA ? o.tay : o.tby, qz = iA ? o.taz : o.tbz;
+                        tx += f2d_bits(qx * imoii); ty += f2d_bits(qy * imoii); tz += f2d_bits(qz * imoii);
+                        if (WRITE && iA) {
+                            const double sum64 = b.R[gA] + b.R[gB];
+                            pe += pair_pe_fp64(M, b.R[gA], b.R[gB], fma(sum64, sum64, -d2_64), d2_64, true, o.k);
+                        }
+                    } else {
+                        const float h = fmaxf(-ovl_s, hmin_s);
+                        const float f = c_vdw * vdw_shape(h, Ras, Rbs);
+                        Fx = f * nx; Fy = f * ny; Fz = f * nz;
+                        if (WRITE && iA) {
+                            const double d2_64 = fp64_d2(b, gA, gB), sum64 = b.R[gA] + b.R[gB];
+                            pe += pair_pe_fp64(M, b.R[gA], b.R[gB], fma(sum64, sum64, -d2_64), d2_64, false, 0.0);
+                        }
+                    }
+                    // acc[A] += F/m[A]; acc[B] -= F/m[B]
+                    fx = iA ? Fx : -Fx; fy = iA ? Fy : -Fy; fz = iA ? Fz : -Fz;
+                };
+                // far pair (or not a pair): its force on i, 0 where it is not
+                // far; returns whether it is close
+                auto far_pair = [&](int t, float& fx, float& fy, float& fz) {
                     const int j = jbase + t;
                     const bool valid = j != i;
                     const float4 q0 = jt.q0[t], q1 = jt.q1[t];
@@ -95,63 +151,13 @@ __device__ double pair_pass_mixed(const Batch& b, int off, int n, const Material
                     const float T = fmaf(-difR, difR, d2);
                     const float P = S * T;
                     const float fr = (cR3i * q1.w) * rcp_approx(P * P);
-                    float fx = fr * rx, fy = fr * ry, fz = fr * rz;
-                    const bool nearp = d2 < b.series_sq * sum2;  // outside the far-pair potential series' range
-                    const bool iA = i > j;
-                    if (valid && d2 < b.far_sq * sum2) {  // close pair
-                        // r = pos[B] - pos[A] in double-float; the sign flips with the orientation
-                        const df::F2 pj[3] = {{q0.x, q1.x}, {q0.y, q1.y}, {q0.z, q1.z}};
-                        df::F2 r3[3];
-#pragma unroll
-                        for (int c = 0; c < 3; ++c) {
-                            const df::F2 pi{pih[c], pil[c]};
-                            r3[c] = iA ? df::sub(pj[c], pi) : df::sub(pi, pj[c]);
-                        }
-                        const df::F2 dd2 = df::add(df::add(df::sqr(r3[0]), df::sqr(r3[1])), df::sqr(r3[2]));
-                        const df::F2 sum = df::add({Ri, Rilo}, {Rj, jt.Rlo[t]});
-                        const df::F2 gap2 = df::sub(df::sqr(sum), dd2);
-                        const float Ras = iA ? Ri : Rj, Rbs = iA ? Rj : Ri;
-                        const float d2s = dd2.hi;
-                        const float inv_d = rsqrtf(d2s);
-                        const float dist_s = d2s * inv_d;
-                        const float ovl_s = __fdividef(gap2.hi, Ras + Rbs + dist_s);
-                        const float nx = r3[0].hi * inv_d, ny = r3[1].hi * inv_d, nz = r3[2].hi * inv_d;
-                        float Fx, Fy, Fz;  // force on A
-                        const int gA = off + (iA ? i : j), gB = off + (iA ? j : i);
-                        if (gap2.hi > 0.0f || (gap2.hi == 0.0f && gap2.lo > 0.0f)) {
-                            ContactIn in;
-                            for (int c = 0; c < 3; ++c) {
-                                in.prevA[c] = b.prev.c[c][gA]; in.prevB[c] = b.prev.c[c][gB];
-                                in.wA[c] = b.w.c[c][gA]; in.wB[c] = b.w.c[c][gB];
-                                in.vA[c] = b.vel.c[c][gA]; in.vB[c] = b.vel.c[c][gB];
-                            }
-                            in.mA = b.m[gA]; in.mB = b.m[gB]; in.kin = kin; in.kout = kout;
-                            // kin/kout: |r|^2 against the previous step's, both FP64 by one formula
-                            const double d2_64 = fp64_d2(b, gA, gB);
-                            const ContactF o = contact_mixed(in, M, sh, d2_64, nx, ny, nz, dist_s * L, ovl_s * L, Ras,
-                                                             Rbs);
-                            Fx = o.fx; Fy = o.fy; Fz = o.fz;
-                            const float qx = iA ? o.tax : o.tbx, qy = iA ? o.tay : o.tby, qz = iA ? o.taz : o.tbz;
-                            tx += f2d_bits(qx * imoii); ty += f2d_bits(qy * imoii); tz += f2d_bits(qz * imoii);
-                            if (WRITE && iA) {
-                                const double sum64 = b.R[gA] + b.R[gB];
-                                pe += pair_pe_fp64(M, b.R[gA], b.R[gB], fma(sum64, sum64, -d2_64), d2_64, true, o.k);
-                            }
-                        } else {
-                            const float h = fmaxf(-ovl_s, hmin_s);
-                            const float f = c_vdw * vdw_shape(h, Ras, Rbs);
-                            Fx = f * nx; Fy = f * ny; Fz = f * nz;
-                            if (WRITE && iA) {
-                                const double d2_64 = fp64_d2(b, gA, gB), sum64 = b.R[gA] + b.R[gB];
-                                pe += pair_pe_fp64(M, b.R[gA], b.R[gB], fma(sum64, sum64, -d2_64), d2_64, false,
-                                                   0.0);
-                            }
-                        }
-                        // acc[A] += F/m[A]; acc[B] -= F/m[B]
-                        fx = iA ? Fx : -Fx; fy = iA ? Fy : -Fy; fz = iA ? Fz : -Fz;
-                    }
-                    if (WRITE && valid && iA && !(d2 < b.far_sq * sum2)) {
-                        if (!nearp) {
+                    const bool close = d2 < b.far_sq * sum2;
+                    const bool use = valid && !close;
+                    fx = use ? fr * rx : 0.0f;
+                    fy = use ? fr * ry : 0.0f;
+                    fz = use ? fr * rz : 0.0f;
+                    if (WRITE && use && i > j) {
+                        if (!(d2 < b.series_sq * sum2)) {
                             pe_far.add(vdw_bracket_far(T, Ri, Rj));
                         } else {  // outside the series' range: FP64, as the close pairs
                             const double d2_64 = fp64_d2(b, off + i, off + j), sum64 = b.R[off + i] + b.R[off + j];
@@ -159,7 +165,34 @@ __device__ double pair_pass_mixed(const Batch& b, int off, int n, const Material
                                                0.0);
                         }
                     }
-                    if (!valid) fx = fy = fz = 0.0f;
+                    return valid && close;
+                };
+                const int jend = min(TILE, n - jbase);
+                float sx = 0, sy = 0, sz = 0;  // this tile's forces on i
+                int t = 0;
+                // four partners at a time, so that their far-pair arithmetic
+                // interleaves; the close ones after, in one branch
+                for (; t + 4 <= jend; t += 4) {
+                    uint32_t closem = 0;
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        float fx, fy, fz;
+                        closem |= (uint32_t)far_pair(t + u, fx, fy, fz) << u;
+                        sx += fx; sy += fy; sz += fz;
+                    }
+                    if (closem) {
+#pragma unroll 1
+                        for (int u = 0; u < 4; ++u)
+                            if ((closem >> u) & 1u) {
+                                float fx, fy, fz;
+                                close_pair(t + u, fx, fy, fz);
+                                sx += fx; sy += fy; sz += fz;
+                            }
+                    }
+                }
+                for (; t < jend; ++t) {
+                    float fx, fy, fz;
+                    if (far_pair(t, fx, fy, fz)) close_pair(t, fx, fy, fz);
                     sx += fx; sy += fy; sz += fz;
                 }
                 ax.add(sx); ay.add(sy); az.add(sz);

@@ -92,3 +92,21 @@ def test_mixed_polydisperse_cluster_energy_tracks_fp64():
     E0 = abs(e0.PE + e0.KE)
     for x, y in zip(ra, rb):
         assert abs(x.E - y.E) <= 1e-6 * E0
+
+
+@pytest.mark.parametrize("spacing", [2.9, 4.6, 9.0])
+def test_mixed_separated_lattice_forces_and_potential(spacing):
+    """Jittered lattices whose nearest pairs sit at about 1.3-1.6, 2.1-2.5
+    and 4.1-5 radii sums, out of contact: every pair takes the FP32 far-pair
+    force path (no square root), and at the two wider spacings every pair's
+    write-step potential comes from the FP32 series of the vdW bracket.
+    Bars: accelerations within 1e-5 of the largest, PE within 5e-6
+    relative."""
+    c = contact_case(343, 21, spacing=spacing, r_spread=0.1)
+    ex, mx = _sim(c, "exact"), _sim(c, "mixed")
+    ee, em = ex.init_conditions(), mx.init_conditions()
+    assert len(ex.contacts()) == 0 and len(mx.contacts()) == 0
+    ge, gm = ex.download(), mx.download()
+    scale = np.abs(ge.acc).max()
+    assert np.abs(gm.acc - ge.acc).max() <= 1e-5 * scale
+    assert abs(em.PE - ee.PE) <= 5e-6 * abs(ee.PE)
