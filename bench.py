@@ -309,15 +309,19 @@ def run_e2e(sim, w, steps: int) -> dict:
     pos[:] = sim.group.pos.reshape(-1); vel[:] = sim.group.vel.reshape(-1); wv[:] = sim.group.w.reshape(-1)
     acc[:] = sim.group.acc.reshape(-1); aacc[:] = sim.group.aacc.reshape(-1); prev[:] = pos
     h = sim.handle
+    # the host buffers stay put: their pointers are formed once, as a C
+    # caller would hold them
     P = _lib.dptr
+    pp, pv, pw, pa, paa, ppr = P(pos), P(vel), P(wv), P(acc), P(aacc), P(prev)
     e = _lib.Energy()
+    pe = ctypes.byref(e)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for k in range(steps):
-        _lib.check(lib.sl_upload_resume(h, P(pos), P(vel), P(wv), P(acc), P(aacc), P(prev)), "sl_upload_resume")
+        _lib.check(lib.sl_upload_resume(h, pp, pv, pw, pa, paa, ppr), "sl_upload_resume")
         prev[:] = pos
-        _lib.check(lib.sl_step(h, 1, int((k + 1) % w.skip == 0), ctypes.byref(e)), "sl_step")
-        _lib.check(lib.sl_download(h, P(pos), P(vel), P(wv), P(acc), P(aacc)), "sl_download")
+        _lib.check(lib.sl_step(h, 1, int((k + 1) % w.skip == 0), pe), "sl_step")
+        _lib.check(lib.sl_download(h, pp, pv, pw, pa, paa), "sl_download")
     el = time.perf_counter() - t0
     return {"value": w.pairs_per_step * steps / el, "unit": UNIT, "h2d_bytes_per_step": 6 * 3 * n * 8,
             "d2h_bytes_per_step": 5 * 3 * n * 8, "steps": steps,

@@ -74,6 +74,9 @@ struct sl_handle {
     unsigned int* h_status = nullptr;
     bool uploaded = false;
     bool forces_ready = false;
+    // the GPU reads and writes pageable host memory directly (cudaDevAttr-
+    // PageableMemoryAccess: coherent CPU-GPU systems such as Grace-Blackwell)
+    bool host_direct = false;
     // graph of one write interval for sl_run
     cudaGraphExec_t interval_exec = nullptr;
     int interval_skip = 0;
@@ -150,6 +153,22 @@ bool all_finite(const double* a, size_t count)
     return bad == 0;
 }
 
+// A device-accessible view of the caller's array p, or NULL where the GPU
+// cannot reach it (plain pageable memory without pageable access): then the
+// exchange goes through the device staging buffer and a copy.
+const double* device_view(const sl_handle* h, const double* p)
+{
+    if (h->host_direct) return p;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();  // clear the failed lookup's error
+        return nullptr;
+    }
+    if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return p;
+    if (a.type == cudaMemoryTypeHost && a.devicePointer) return static_cast<const double*>(a.devicePointer);
+    return nullptr;
+}
+
 // The six vec3 arrays a handle exchanges with its caller, in staging order.
 void stage_arrays(sl_handle* h, sl::Vec3Soa* out[6])
 {
@@ -190,6 +209,9 @@ int sl_create(int n, const sl_material* mat, int mode, sl_handle** out)
     if (e != cudaSuccess) { delete h; return cuda_fail(e, "cudaGetDevice"); }
     e = cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
     if (e != cudaSuccess) { delete h; return cuda_fail(e, "cudaDeviceGetAttribute"); }
+    int pageable = 0;
+    if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, h->device) == cudaSuccess)
+        h->host_direct = pageable != 0;
     e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) { delete h; return cuda_fail(e, "cudaStreamCreate"); }
     if (mode == SL_MODE_EXACT) {
@@ -355,19 +377,26 @@ int sl_upload_resume(sl_handle* h, const double* pos, const double* vel, const d
     if (!all_finite(pos, 3 * (size_t)n) || !all_finite(vel, 3 * (size_t)n) || !all_finite(w, 3 * (size_t)n))
         return fail(SL_ERR_ARG, "non-finite position, velocity or spin in input");
     const size_t np = h->sys.npad;
-    // one copy per array into the device staging area; absent acc/aacc are
-    // zero, an absent previous position is the position
+    // the staging kernel reads each array where the GPU can reach it, else
+    // from a copy in the device staging area; absent acc/aacc are zero, an
+    // absent previous position is the position
     const double* srcs[6] = {pos, vel, w, acc, aacc, pos_prev};
+    const double* views[6] = {};
     unsigned present = 0;
     for (int k = 0; k < 6; ++k)
         if (srcs[k]) {
-            SL_CUDA(cudaMemcpyAsync(h->d_stage + (size_t)k * 3 * np, srcs[k], 3 * (size_t)n * sizeof(double),
-                                    cudaMemcpyHostToDevice, h->stream));
+            views[k] = device_view(h, srcs[k]);
+            if (!views[k]) {
+                double* stage = h->d_stage + (size_t)k * 3 * np;
+                SL_CUDA(cudaMemcpyAsync(stage, srcs[k], 3 * (size_t)n * sizeof(double), cudaMemcpyHostToDevice,
+                                        h->stream));
+                views[k] = stage;
+            }
             present |= 1u << k;
         }
     sl::Vec3Soa* dst[6];
     stage_arrays(h, dst);
-    sl::launch_stage_in(h->sys, h->d_stage, dst, present, h->stream);
+    sl::launch_stage_in(h->sys, views, dst, present, h->stream);
     SL_CUDA(cudaGetLastError());
     SL_CUDA(cudaMemsetAsync(h->sys.status, 0, sizeof(unsigned int), h->stream));
     SL_CUDA(cudaStreamSynchronize(h->stream));
@@ -470,12 +499,23 @@ int sl_download(sl_handle* h, double* pos, double* vel, double* w, double* acc, 
         if (outs[k]) want |= 1u << k;
     sl::Vec3Soa* src[6];
     stage_arrays(h, src);
-    sl::launch_stage_out(h->sys, h->d_stage, src, want, h->stream);
+    // written where the GPU can reach the caller's array, else staged and copied
+    double* views[6] = {};
+    bool staged[5] = {};
+    for (int k = 0; k < 5; ++k)
+        if (outs[k]) {
+            views[k] = const_cast<double*>(device_view(h, outs[k]));
+            if (!views[k]) {
+                views[k] = h->d_stage + (size_t)k * 3 * np;
+                staged[k] = true;
+            }
+        }
+    sl::launch_stage_out(h->sys, views, src, want, h->stream);
     SL_CUDA(cudaGetLastError());
     for (int k = 0; k < 5; ++k)
-        if (outs[k])
-            SL_CUDA(cudaMemcpyAsync(outs[k], h->d_stage + (size_t)k * 3 * np, 3 * (size_t)n * sizeof(double),
-                                    cudaMemcpyDeviceToHost, h->stream));
+        if (staged[k])
+            SL_CUDA(cudaMemcpyAsync(outs[k], views[k], 3 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost,
+                                    h->stream));
     SL_CUDA(cudaStreamSynchronize(h->stream));
     return SL_OK;
 }

@@ -26,13 +26,14 @@ struct StepOverlap {
 };
 
 void launch_derive(const System& s, cudaStream_t st);
-// vec3[n] AoS copies in stage (array k at stage + 3 k npad) <-> the SoA
-// arrays arr[k]: in, for the arrays whose bit is set in `present` (others:
-// arr[5], the previous positions, takes the positions; the rest zero);
-// out, for the arrays whose bit is set in `want`.
-void launch_stage_in(const System& s, const double* stage, Vec3Soa* const arr[6], unsigned present,
+// vec3[n] AoS arrays src[k] / dst[k] (device-accessible: device staging,
+// or host memory the GPU reads and writes directly) <-> the SoA arrays
+// arr[k]: in, for the arrays whose bit is set in `present` (others: arr[5],
+// the previous positions, takes the positions; the rest zero); out, for the
+// arrays whose bit is set in `want`.
+void launch_stage_in(const System& s, const double* const src[6], Vec3Soa* const arr[6], unsigned present,
                      cudaStream_t st);
-void launch_stage_out(const System& s, double* stage, Vec3Soa* const arr[6], unsigned want, cudaStream_t st);
+void launch_stage_out(const System& s, double* const dst[6], Vec3Soa* const arr[6], unsigned want, cudaStream_t st);
 // map: a tensor map of the pair-term buffer (make_pair_map) selects the
 // TMA-streamed row sums; NULL the plain-load form.
 void launch_step(const System& s, bool write, int num_sms, cudaStream_t st, StepTimers* tm,

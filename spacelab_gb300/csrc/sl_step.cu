@@ -380,34 +380,39 @@ struct StageArrays {
     Vec3Soa a[6];
 };
 
-__global__ void stage_in_kernel(const __grid_constant__ System s, const double* __restrict__ stage,
+// The caller's vec3[n] AoS arrays (x, y, z per sphere), one pointer each:
+// host memory the kernel reads or writes directly, or device staging.
+struct StagePtrs {
+    const double* p[6];
+};
+
+__global__ void stage_in_kernel(const __grid_constant__ System s, const __grid_constant__ StagePtrs src,
                                 const __grid_constant__ StageArrays arr, unsigned present)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= s.npad) return;
-    const size_t np = s.npad;
     const bool real = i < s.n;
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
-        const int src = (k == 5 && !(present & 32u)) ? 0 : k;  // previous positions default to the positions
-        const bool have = (present >> src) & 1u;
+        const int from = (k == 5 && !(present & 32u)) ? 0 : k;  // previous positions default to the positions
+        const bool have = real && ((present >> from) & 1u);
+        const double* in = src.p[from];
 #pragma unroll
-        for (int c = 0; c < 3; ++c)
-            arr.a[k].c[c][i] = (real && have) ? stage[src * 3 * np + 3 * (size_t)i + c] : 0.0;
+        for (int c = 0; c < 3; ++c) arr.a[k].c[c][i] = have ? in[3 * (size_t)i + c] : 0.0;
     }
 }
 
-__global__ void stage_out_kernel(const __grid_constant__ System s, double* __restrict__ stage,
+__global__ void stage_out_kernel(const __grid_constant__ System s, const __grid_constant__ StagePtrs dst,
                                  const __grid_constant__ StageArrays arr, unsigned want)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= s.n) return;
-    const size_t np = s.npad;
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
         if (!((want >> k) & 1u)) continue;
+        double* out = const_cast<double*>(dst.p[k]);
 #pragma unroll
-        for (int c = 0; c < 3; ++c) stage[k * 3 * np + 3 * (size_t)i + c] = arr.a[k].c[c][i];
+        for (int c = 0; c < 3; ++c) out[3 * (size_t)i + c] = arr.a[k].c[c][i];
     }
 }
 
@@ -439,19 +444,27 @@ void launch_derive(const System& s, cudaStream_t st)
     derive_kernel<<<(s.npad + 255) / 256, 256, 0, st>>>(s);
 }
 
-void launch_stage_in(const System& s, const double* stage, Vec3Soa* const arr[6], unsigned present,
+void launch_stage_in(const System& s, const double* const src[6], Vec3Soa* const arr[6], unsigned present,
                      cudaStream_t st)
 {
     StageArrays a;
-    for (int k = 0; k < 6; ++k) a.a[k] = *arr[k];
-    stage_in_kernel<<<(s.npad + 255) / 256, 256, 0, st>>>(s, stage, a, present);
+    StagePtrs p;
+    for (int k = 0; k < 6; ++k) {
+        a.a[k] = *arr[k];
+        p.p[k] = src[k];
+    }
+    stage_in_kernel<<<(s.npad + 255) / 256, 256, 0, st>>>(s, p, a, present);
 }
 
-void launch_stage_out(const System& s, double* stage, Vec3Soa* const arr[6], unsigned want, cudaStream_t st)
+void launch_stage_out(const System& s, double* const dst[6], Vec3Soa* const arr[6], unsigned want, cudaStream_t st)
 {
     StageArrays a;
-    for (int k = 0; k < 6; ++k) a.a[k] = *arr[k];
-    stage_out_kernel<<<(s.n + 255) / 256, 256, 0, st>>>(s, stage, a, want);
+    StagePtrs p;
+    for (int k = 0; k < 6; ++k) {
+        a.a[k] = *arr[k];
+        p.p[k] = dst[k];
+    }
+    stage_out_kernel<<<(s.n + 255) / 256, 256, 0, st>>>(s, p, a, want);
 }
 
 void launch_drift(const System& s, cudaStream_t st)
