@@ -386,34 +386,34 @@ struct StagePtrs {
     const double* p[6];
 };
 
+// One thread per element of the flattened vec3[n] arrays (sphere t / 3,
+// component t % 3), so that the caller-side accesses are contiguous -- they
+// may cross the CPU-GPU link -- and the gather / scatter falls on the SoA
+// arrays in HBM.
 __global__ void stage_in_kernel(const __grid_constant__ System s, const __grid_constant__ StagePtrs src,
                                 const __grid_constant__ StageArrays arr, unsigned present)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= s.npad) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 3 * s.npad) return;
+    const int i = t / 3, c = t - 3 * (t / 3);
     const bool real = i < s.n;
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
         const int from = (k == 5 && !(present & 32u)) ? 0 : k;  // previous positions default to the positions
         const bool have = real && ((present >> from) & 1u);
-        const double* in = src.p[from];
-#pragma unroll
-        for (int c = 0; c < 3; ++c) arr.a[k].c[c][i] = have ? in[3 * (size_t)i + c] : 0.0;
+        arr.a[k].c[c][i] = have ? src.p[from][t] : 0.0;
     }
 }
 
 __global__ void stage_out_kernel(const __grid_constant__ System s, const __grid_constant__ StagePtrs dst,
                                  const __grid_constant__ StageArrays arr, unsigned want)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= s.n) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 3 * s.n) return;
+    const int i = t / 3, c = t - 3 * (t / 3);
 #pragma unroll
-    for (int k = 0; k < 6; ++k) {
-        if (!((want >> k) & 1u)) continue;
-        double* out = const_cast<double*>(dst.p[k]);
-#pragma unroll
-        for (int c = 0; c < 3; ++c) out[3 * (size_t)i + c] = arr.a[k].c[c][i];
-    }
+    for (int k = 0; k < 6; ++k)
+        if ((want >> k) & 1u) const_cast<double*>(dst.p[k])[t] = arr.a[k].c[c][i];
 }
 
 // ------------------------------------------------------------ launchers --
@@ -453,7 +453,7 @@ void launch_stage_in(const System& s, const double* const src[6], Vec3Soa* const
         a.a[k] = *arr[k];
         p.p[k] = src[k];
     }
-    stage_in_kernel<<<(s.npad + 255) / 256, 256, 0, st>>>(s, p, a, present);
+    stage_in_kernel<<<(3 * s.npad + 255) / 256, 256, 0, st>>>(s, p, a, present);
 }
 
 void launch_stage_out(const System& s, double* const dst[6], Vec3Soa* const arr[6], unsigned want, cudaStream_t st)
@@ -464,7 +464,7 @@ void launch_stage_out(const System& s, double* const dst[6], Vec3Soa* const arr[
         a.a[k] = *arr[k];
         p.p[k] = dst[k];
     }
-    stage_out_kernel<<<(s.n + 255) / 256, 256, 0, st>>>(s, p, a, want);
+    stage_out_kernel<<<(3 * s.n + 255) / 256, 256, 0, st>>>(s, p, a, want);
 }
 
 void launch_drift(const System& s, cudaStream_t st)
