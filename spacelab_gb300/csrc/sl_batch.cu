@@ -179,12 +179,14 @@ __global__ void batch_derive_kernel(const __grid_constant__ Batch b)
     b.cR3[i] = b.mat.Ha / 6 * 64 * R * R * R;
     b.rm[i] = recip_of(m);
     b.inv_moi[i] = 1.0 / moi;
-    if (b.f_R) {
-        const float rh = d2f_bits(R, b.len_shift);
+    if (b.f_R) {  // mixed form: slot i holds sphere perm[i]
+        const int g = b.perm[i];
+        const double Rg = b.R[g];
+        const float rh = d2f_bits(Rg, b.len_shift);
         b.f_R[i] = rh;
-        b.f_Rlo[i] = d2f_bits(R - f2d_bits(rh) * ldexp(1.0, b.len_shift), b.len_shift);
-        b.f_inv_m[i] = d2f_bits(1.0 / m, 0);
-        b.f_inv_moi[i] = d2f_bits(1.0 / moi, 0);
+        b.f_Rlo[i] = d2f_bits(Rg - f2d_bits(rh) * ldexp(1.0, b.len_shift), b.len_shift);
+        b.f_inv_m[i] = d2f_bits(1.0 / b.m[g], 0);
+        b.f_inv_moi[i] = d2f_bits(1.0 / b.moi[g], 0);
     }
 }
 

@@ -24,15 +24,17 @@ struct Batch {
     double *R, *m, *moi, *twoR, *fourR, *cR3;
     unsigned long long* rm;  // 64-bit fixed-point reciprocal significand of m (recip_sig)
     double* inv_moi;
-    float *f_R, *f_inv_m, *f_inv_moi;  // mixed form (lengths scaled by 2^-len_shift)
-    // mixed form: the radii's double-float lo parts, and the positions as
-    // double-float hi (x, y, z) and lo (x, y, z), written by the drift
-    float *f_Rlo, *f_pos[6];
-    // mixed form: the order in which the pair pass assigns spheres to
-    // threads, perm[off + k] = off + the instance's k-th sphere in Z-order of
-    // its positions at upload, so that a warp's spheres are close together
-    // and few warps take the near-pair path for a given partner
+    // Mixed form.  Its pair passes see each instance's spheres in "slots":
+    // perm[off + k] = off + the instance's k-th sphere in Z-order of its
+    // positions at upload, so that a warp's spheres, and a 32-slot block, are
+    // close together and few of them take the close-pair path.  The FP32
+    // arrays below are in slot order (entry off + k belongs to sphere
+    // perm[off + k]); the FP64 state stays in the caller's order.
     const int* perm;
+    float *f_R, *f_inv_m, *f_inv_moi;  // lengths scaled by 2^-len_shift
+    // the radii's double-float lo parts, and the positions as double-float
+    // hi (x, y, z) and lo (x, y, z), written by the drift
+    float *f_Rlo, *f_pos[6];
     float far_sq, series_sq;  // far-pair thresholds (far_thresholds in sl_pair_mixed.cuh)
     int len_shift;
     Material mat;         // G, Ha, u_r, h_min shared; u_s per instance

@@ -30,7 +30,7 @@ __device__ __forceinline__ void cta_sum8(double v[8], double (*sh)[32])
 __device__ __forceinline__ void drift(const Batch& b, int off, int n, double dt)
 {
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const int g = off + i;
+        const int g = b.perm ? b.perm[off + i] : off + i;  // the mixed form walks slots (sl_batch.h)
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             const double vh = b.vel.c[c][g] + (.5 * b.acc.c[c][g]) * dt;   // :84
@@ -41,14 +41,14 @@ __device__ __forceinline__ void drift(const Batch& b, int off, int n, double dt)
             b.prev.c[c][g] = p;
             b.pos.c[c][g] = p + vh * dt;                                   // :90
         }
-        if (b.f_pos[0]) {  // mixed form: scaled positions as double-float hi + lo
+        if (b.f_pos[0]) {  // mixed form: scaled positions as double-float hi + lo, in slot off + i
             const double scale = ldexp(1.0, b.len_shift);
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
                 const double p = b.pos.c[c][g];
                 const float hi = d2f_bits(p, b.len_shift);
-                b.f_pos[c][g] = hi;
-                b.f_pos[3 + c][g] = d2f_bits(p - f2d_bits(hi) * scale, b.len_shift);
+                b.f_pos[c][off + i] = hi;
+                b.f_pos[3 + c][off + i] = d2f_bits(p - f2d_bits(hi) * scale, b.len_shift);
             }
         }
     }

@@ -24,6 +24,7 @@ struct JTileM {
     float4 q0[TILE];  // scaled position hi x, y, z and scaled radius R
     float4 q1[TILE];  // scaled position lo x, y, z and R^3
     float Rlo[TILE];  // the radius's double-float lo part
+    int idx[TILE];    // the sphere's index in the instance (its slot's perm entry)
 };
 
 // |pos[gB] - pos[gA]|^2 in FP64, the previous-step formula of contact_mixed
@@ -56,32 +57,34 @@ __device__ double pair_pass_mixed(const Batch& b, int off, int n, const Material
     df::Sum pe_far{0.0f, 0.0f};  // far pairs' vdW brackets (write steps, i = A)
     for (int ibase = 0; ibase < n; ibase += blockDim.x) {
         const bool active = ibase + threadIdx.x < n;
-        const int gi = active ? b.perm[off + ibase + threadIdx.x] : off;  // Z-order: a warp's spheres are close
+        const int si = off + (active ? ibase + threadIdx.x : 0);  // slot: Z-order, a warp's spheres are close
+        const int gi = b.perm[si];
         const int i = gi - off;
-        const float pih[3] = {b.f_pos[0][gi], b.f_pos[1][gi], b.f_pos[2][gi]};
-        const float pil[3] = {b.f_pos[3][gi], b.f_pos[4][gi], b.f_pos[5][gi]};
-        const float Ri = b.f_R[gi], Rilo = b.f_Rlo[gi];
+        const float pih[3] = {b.f_pos[0][si], b.f_pos[1][si], b.f_pos[2][si]};
+        const float pil[3] = {b.f_pos[3][si], b.f_pos[4][si], b.f_pos[5][si]};
+        const float Ri = b.f_R[si], Rilo = b.f_Rlo[si];
         const float cR3i = c_vdw * (Ri * Ri * Ri);
-        const float imoii = b.f_inv_moi[gi];
+        const float imoii = b.f_inv_moi[si];
         df::Sum ax{0.0f, 0.0f}, ay{0.0f, 0.0f}, az{0.0f, 0.0f};
         double tx = 0, ty = 0, tz = 0;
         for (int jbase = 0; jbase < n; jbase += TILE) {
             for (int t = threadIdx.x; t < TILE; t += blockDim.x) {
                 const int j = jbase + t;
                 if (j < n) {
-                    const int g = off + j;
+                    const int g = off + j;  // slot
                     const float r = b.f_R[g];
                     jt.q0[t] = make_float4(b.f_pos[0][g], b.f_pos[1][g], b.f_pos[2][g], r);
                     jt.q1[t] = make_float4(b.f_pos[3][g], b.f_pos[4][g], b.f_pos[5][g], r * r * r);
                     jt.Rlo[t] = b.f_Rlo[g];
+                    jt.idx[t] = b.perm[g] - off;
                 }
             }
             __syncthreads();
             if (active) {
-                // close pair j = jbase + t: double-float geometry, contact or
+                // close pair in slot jbase + t: double-float geometry, contact or
                 // clamped vdW in the pair's (A, B) orientation; the force on i
                 auto close_pair = [&](int t, float& fx, float& fy, float& fz) {
-                    const int j = jbase + t;
+                    const int j = jt.idx[t];
                     const bool iA = i > j;
                     const float4 q0 = jt.q0[t], q1 = jt.q1[t];
                     const float Rj = q0.w;
@@ -137,7 +140,7 @@ __device__ double pair_pass_mixed(const Batch& b, int off, int n, const Material
                 // far pair (or not a pair): its force on i, 0 where it is not
                 // far; returns whether it is close
                 auto far_pair = [&](int t, float& fx, float& fy, float& fz) {
-                    const int j = jbase + t;
+                    const int j = jt.idx[t];
                     const bool valid = j != i;
                     const float4 q0 = jt.q0[t], q1 = jt.q1[t];
                     const float Rj = q0.w;
@@ -200,7 +203,7 @@ __device__ double pair_pass_mixed(const Batch& b, int off, int n, const Material
             __syncthreads();
         }
         if (active) {
-            const double imi = f2d_bits(b.f_inv_m[gi]);
+            const double imi = f2d_bits(b.f_inv_m[si]);
             b.acc.c[0][gi] = (f2d_bits(ax.s) + f2d_bits(ax.c)) * imi;
             b.acc.c[1][gi] = (f2d_bits(ay.s) + f2d_bits(ay.c)) * imi;
             b.acc.c[2][gi] = (f2d_bits(az.s) + f2d_bits(az.c)) * imi;
