@@ -36,12 +36,20 @@ struct Batch {
     // hi (x, y, z) and lo (x, y, z), written by the drift
     float *f_Rlo, *f_pos[6];
     float far_sq, series_sq;  // far-pair thresholds (far_thresholds in sl_pair_mixed.cuh)
+    // mixed form, pair-tile pass (shape tile 0): per-CTA scratch of tile
+    // partials, CTA c at part + c * part_cta, [6][part_nb][part_np] floats
+    float* part;
+    size_t part_cta;
+    int part_nb, part_np, part_ctas;
     int len_shift;
     Material mat;         // G, Ha, u_r, h_min shared; u_s per instance
     double* energy;       // [ninst][nrec][8]
     int nrec;
     unsigned* status;     // per instance: 1 = non-finite state
 };
+
+// CTAs per SM the pair-tile pass's scratch is sized for.
+constexpr int kTileCtasPerSm = 4;
 
 // Launch the persistent kernel over all instances: an initial force pass
 // when do_init, then steps first_step .. first_step+nsteps-1 with a write

@@ -28,7 +28,7 @@ namespace {
 
 size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
-const int kTiles[3] = {32, 64, 128};
+const int kTiles[4] = {32, 64, 128, 0};  // 0: the mixed form's pair-tile pass
 const int kThreads[3] = {64, 128, 256};
 
 }  // namespace
@@ -54,6 +54,7 @@ int blocks_for(const sl_batch* h, int tile, int threads)
     int per_sm = sl::batch_max_blocks_per_sm(tile, threads, h->mode == SL_MODE_MIXED);
     if (per_sm < 1) per_sm = 1;
     long long blocks = (long long)per_sm * h->num_sms;
+    if (tile == 0 && blocks > h->b.part_ctas) blocks = h->b.part_ctas;  // one scratch region per CTA
     if (blocks > h->b.ninst) blocks = h->b.ninst;
     return (int)blocks;
 }
@@ -202,6 +203,13 @@ int sl_batch_create(int ninst, const int* counts, const sl_material* mat, int mo
     const size_t o_st = take(ninst * sizeof(unsigned));
     const size_t o_snap = take(15 * T * sizeof(double));
     const size_t o_perm = take(mode == SL_MODE_MIXED ? T * sizeof(int) : 0);
+    // mixed: the pair-tile pass's per-CTA partials, sized for the largest instance
+    const int max_n = *std::max_element(counts, counts + ninst);
+    b.part_nb = (max_n + sl::kBlock - 1) / sl::kBlock;
+    b.part_np = b.part_nb * sl::kBlock;
+    b.part_cta = 6 * (size_t)b.part_nb * b.part_np;
+    b.part_ctas = h->num_sms * sl::kTileCtasPerSm;
+    const size_t o_part = take(mode == SL_MODE_MIXED ? b.part_cta * b.part_ctas * sizeof(float) : 0);
     h->arena_bytes = off;
     if (cudaMalloc(&h->arena, off) != cudaSuccess) {
         sl_batch_destroy(h);
@@ -222,6 +230,7 @@ int sl_batch_create(int ninst, const int* counts, const sl_material* mat, int mo
         b.f_Rlo = reinterpret_cast<float*>(base + o_f[3]);
         for (int k = 0; k < 6; ++k) b.f_pos[k] = reinterpret_cast<float*>(base + o_f[4 + k]);
         b.perm = reinterpret_cast<const int*>(base + o_perm);
+        b.part = reinterpret_cast<float*>(base + o_part);
     }
     int* order = reinterpret_cast<int*>(base + o_order);
     int* doff = reinterpret_cast<int*>(base + o_off);
@@ -321,8 +330,9 @@ int sl_batch_upload(sl_batch* h, const double* pos, const double* vel, const dou
 int sl_batch_set_shape(sl_batch* h, int tile, int threads)
 {
     if (!h) return sl_record_error(SL_ERR_ARG, "null batch");
-    if ((tile != 32 && tile != 64 && tile != 128) || (threads != 64 && threads != 128 && threads != 256))
-        return sl_record_error(SL_ERR_ARG, "tile must be 32/64/128 and threads 64/128/256");
+    if ((tile != 32 && tile != 64 && tile != 128 && tile != 0) || (threads != 64 && threads != 128 && threads != 256))
+        return sl_record_error(SL_ERR_ARG, "tile must be 32/64/128 (or 0) and threads 64/128/256");
+    if (tile == 0 && h->mode != SL_MODE_MIXED) return sl_record_error(SL_ERR_ARG, "tile 0 is the mixed form's");
     h->tile = tile;
     h->threads = threads;
     return SL_OK;
@@ -338,8 +348,12 @@ int sl_batch_autotune(sl_batch* h, int sample_steps, int* tile, int* threads, do
     SLB_CUDA(cudaEventCreate(&e1));
     float best = 1e30f;
     int bt = h->tile, bth = h->threads, k = 0;
-    for (int ti = 0; ti < 3; ++ti)
+    for (int ti = 0; ti < 4; ++ti)
         for (int hi = 0; hi < 3; ++hi, ++k) {
+            if (kTiles[ti] == 0 && h->mode != SL_MODE_MIXED) {
+                if (times_ms) times_ms[k] = -1.0;
+                continue;
+            }
             if (int r = snapshot_copy(h, false)) return r;
             // first launch compiles nothing but warms the caches; time the second
             if (int r = launch_run(h, kTiles[ti], kThreads[hi], 1, 1, 0, 0)) return r;

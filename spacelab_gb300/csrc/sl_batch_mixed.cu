@@ -12,6 +12,8 @@
 #include "sl_df.cuh"
 #include "sl_pair_mixed.cuh"
 
+#include <type_traits>
+
 namespace sl {
 
 namespace {
@@ -259,12 +261,279 @@ __global__ void __launch_bounds__(256) batch_mixed_kernel(const __grid_constant_
     }
 }
 
+// ---------------------------------------------------------------------------
+// Pair-tile pass: every unordered pair once.  The CTA's warps take the
+// instance's lower-triangular 32 x 32 slot-block tiles in turn and sweep
+// each diagonally as the all-pairs mixed kernel does (sl_step_mixed.cu): at
+// step k lane b takes (row (b + k) mod 32, column b), its column sum stays in
+// a register and each row sum moves one lane down per step.  A tile writes one
+// FP32 partial per sphere and component -- forces and torques -- to the CTA's
+// scratch part[6][nb][np] (slot-indexed), and the CTA then adds each sphere's
+// partials over the partner blocks in ascending order in compensated sums.
+// Torques exist only in contact: a row sphere's arrive by shared-memory adds
+// (one lane per row in a step, the steps in program order, so the order is
+// fixed), a column sphere's in a register.
+constexpr int kRowStrideT = 12;  // floats per row sphere: hi xyz R | lo xyz cR3 | Rlo 1/m 1/moi index
+constexpr int kTileWarps = 8;
+
+struct TileSmem {
+    float rows[kTileWarps][kBlock * kRowStrideT];
+    float rowtq[kTileWarps][3 * kBlock];
+};
+
+template <bool WRITE>
+__device__ double tile_pass_mixed(const Batch& b, int off, int n, const Material& M, double kin, double kout,
+                                  TileSmem& sm)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int sh = b.len_shift;
+    const float L = ldexpf(1.0f, sh);
+    const float hmin_s = (float)M.h_min / L;
+    const float c_vdw = (float)(M.Ha / 6 * 64) / L;
+    const int nbk = (n + kBlock - 1) / kBlock;
+    const long long ntiles = (long long)nbk * (nbk + 1) / 2;
+    float* part = b.part + (size_t)blockIdx.x * b.part_cta;
+    const size_t pplane = (size_t)b.part_nb * b.part_np;
+    float* rows = sm.rows[warp];
+    float* rowtq = sm.rowtq[warp];
+    const int nxt = (lane + 1) & (kBlock - 1);
+    double pe = 0;
+    df::Sum pe_far{0.0f, 0.0f};  // far pairs' vdW brackets (write steps)
+    for (long long t = warp; t < ntiles; t += nwarps) {
+        int X, Y;
+        tile_coords(t, X, Y);
+        {
+            const int sA = off + min(X * kBlock + lane, n - 1);  // slot (padding rows repeat the last)
+            const float Ri = b.f_R[sA];
+            float* row = rows + lane * kRowStrideT;
+            *reinterpret_cast<float4*>(row) = make_float4(b.f_pos[0][sA], b.f_pos[1][sA], b.f_pos[2][sA], Ri);
+            *reinterpret_cast<float4*>(row + 4) =
+                make_float4(b.f_pos[3][sA], b.f_pos[4][sA], b.f_pos[5][sA], c_vdw * (Ri * Ri * Ri));
+            row[8] = b.f_Rlo[sA];
+            row[9] = b.f_inv_m[sA];
+            row[10] = b.f_inv_moi[sA];
+            row[11] = __int_as_float(b.perm[sA] - off);
+            rowtq[lane] = 0.0f; rowtq[kBlock + lane] = 0.0f; rowtq[2 * kBlock + lane] = 0.0f;
+        }
+        __syncwarp();
+        const int sB = Y * kBlock + lane;  // slot in the instance
+        const bool bvalid = sB < n;
+        const int gBs = off + min(sB, n - 1);
+        const float bx = b.f_pos[0][gBs], by = b.f_pos[1][gBs], bz = b.f_pos[2][gBs];
+        const float bxl = b.f_pos[3][gBs], byl = b.f_pos[4][gBs], bzl = b.f_pos[5][gBs];
+        const float Rbs = b.f_R[gBs], Rblo = b.f_Rlo[gBs], inv_mb = b.f_inv_m[gBs], imoib = b.f_inv_moi[gBs];
+        const int iB = b.perm[gBs] - off;  // the column sphere's index in the instance
+        const float Rb3 = Rbs * Rbs * Rbs;
+        const int nA = n - X * kBlock;
+        float ax = 0, ay = 0, az = 0;        // running sum of row (lane + k) mod 32 at step k
+        float bsx = 0, bsy = 0, bsz = 0;     // the column sphere's force sum
+        float ctx = 0, cty = 0, ctz = 0;     // the column sphere's torque sum
+        // close pair (row r, this lane's column): double-float geometry, then
+        // the contact branch in the reference's orientation (A = the larger
+        // index in the instance) or the clamped vdW; the force on the row sphere
+        auto close_pair = [&](int r, float& fx, float& fy, float& fz) {
+            const float4 q0 = *reinterpret_cast<const float4*>(rows + r * kRowStrideT);
+            const float4 q1 = *reinterpret_cast<const float4*>(rows + r * kRowStrideT + 4);
+            const float Ras = q0.w;
+            const int iA = __float_as_int(rows[r * kRowStrideT + 11]);
+            const df::F2 drx = df::sub({bx, bxl}, {q0.x, q1.x});
+            const df::F2 dry = df::sub({by, byl}, {q0.y, q1.y});
+            const df::F2 drz = df::sub({bz, bzl}, {q0.z, q1.z});
+            const df::F2 dd2 = df::add(df::add(df::sqr(drx), df::sqr(dry)), df::sqr(drz));
+            const df::F2 sum = df::add({Ras, rows[r * kRowStrideT + 8]}, {Rbs, Rblo});
+            const df::F2 gap2 = df::sub(df::sqr(sum), dd2);
+            const float d2s = dd2.hi;
+            const float inv_dn = rsqrtf(d2s);
+            const float dist_s = d2s * inv_dn;
+            const float ovl_s = __fdividef(gap2.hi, Ras + Rbs + dist_s);
+            const float nx = drx.hi * inv_dn, ny = dry.hi * inv_dn, nz = drz.hi * inv_dn;  // row -> column
+            const bool rowA = iA > iB;
+            const int gA = off + (rowA ? iA : iB), gB = off + (rowA ? iB : iA);
+            if (gap2.hi > 0.0f || (gap2.hi == 0.0f && gap2.lo > 0.0f)) {
+                ContactIn in;
+                for (int c = 0; c < 3; ++c) {
+                    in.prevA[c] = b.prev.c[c][gA]; in.prevB[c] = b.prev.c[c][gB];
+                    in.wA[c] = b.w.c[c][gA]; in.wB[c] = b.w.c[c][gB];
+                    in.vA[c] = b.vel.c[c][gA]; in.vB[c] = b.vel.c[c][gB];
+                }
+                in.mA = b.m[gA]; in.mB = b.m[gB]; in.kin = kin; in.kout = kout;
+                // kin/kout: |r|^2 against the previous step's, both FP64 by one formula
+                const double d2_64 = fp64_d2(b, gA, gB);
+                const float sg = rowA ? 1.0f : -1.0f;  // unit vector A -> B
+                const ContactF o = contact_mixed(in, M, sh, d2_64, sg * nx, sg * ny, sg * nz, dist_s * L, ovl_s * L,
+                                                 rowA ? Ras : Rbs, rowA ? Rbs : Ras);
+                fx = sg * o.fx; fy = sg * o.fy; fz = sg * o.fz;  // o.f acts on A; B takes -o.f
+                const float imoia = rows[r * kRowStrideT + 10];
+                atomicAdd(&rowtq[r], (rowA ? o.tax : o.tbx) * imoia);
+                atomicAdd(&rowtq[kBlock + r], (rowA ? o.tay : o.tby) * imoia);
+                atomicAdd(&rowtq[2 * kBlock + r], (rowA ? o.taz : o.tbz) * imoia);
+                ctx += (rowA ? o.tbx : o.tax) * imoib;
+                cty += (rowA ? o.tby : o.tay) * imoib;
+                ctz += (rowA ? o.tbz : o.taz) * imoib;
+                if (WRITE) {
+                    const double sum64 = b.R[gA] + b.R[gB];
+                    pe += pair_pe_fp64(M, b.R[gA], b.R[gB], fma(sum64, sum64, -d2_64), d2_64, true, o.k);
+                }
+                return;
+            }
+            const float hn = fmaxf(-ovl_s, hmin_s);
+            const float f = c_vdw * vdw_shape(hn, Ras, Rbs);
+            fx = f * nx; fy = f * ny; fz = f * nz;
+            if (WRITE) {
+                const double d2_64 = fp64_d2(b, gA, gB), sum64 = b.R[gA] + b.R[gB];
+                pe += pair_pe_fp64(M, b.R[gA], b.R[gB], fma(sum64, sum64, -d2_64), d2_64, false, 0.0);
+            }
+        };
+        auto sweep = [&](auto full_tag) {
+            constexpr bool FULL = decltype(full_tag)::value;
+#pragma unroll 2
+            for (int k = 0; k < kBlock; ++k) {
+                const int r = (lane + k) & (kBlock - 1);
+                const bool valid = FULL || (bvalid && r < nA && (X != Y || lane < r));
+                const float4 q0 = *reinterpret_cast<const float4*>(rows + r * kRowStrideT);
+                const float4 q1 = *reinterpret_cast<const float4*>(rows + r * kRowStrideT + 4);
+                const float Ras = q0.w;
+                // far pair: vdW without a square root (sl_step_mixed.cu)
+                const float rx = (bx - q0.x) + (bxl - q1.x);
+                const float ry = (by - q0.y) + (byl - q1.y);
+                const float rz = (bz - q0.z) + (bzl - q1.z);
+                const float d2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
+                const float sumR = Ras + Rbs, difR = Ras - Rbs;
+                const float sum2 = sumR * sumR;
+                const float S = d2 - sum2;
+                const float T = fmaf(-difR, difR, d2);
+                const float P = S * T;
+                const float fr = (q1.w * Rb3) * rcp_approx(P * P);  // |F| / |r|
+                float fx = fr * rx, fy = fr * ry, fz = fr * rz;
+                const bool close = d2 < b.far_sq * sum2;
+                if (valid && close) close_pair(r, fx, fy, fz);
+                if (WRITE && valid && !close) {
+                    if (!(d2 < b.series_sq * sum2)) {
+                        pe_far.add(vdw_bracket_far(T, Ras, Rbs));
+                    } else {  // outside the series' range: FP64, as the close pairs
+                        const int iA = __float_as_int(rows[r * kRowStrideT + 11]);
+                        const double d2_64 = fp64_d2(b, off + iA, off + iB), sum64 = b.R[off + iA] + b.R[off + iB];
+                        pe += pair_pe_fp64(M, b.R[off + iA], b.R[off + iB], fma(sum64, sum64, -d2_64), d2_64, false,
+                                           0.0);
+                    }
+                }
+                if (!FULL && !valid) fx = fy = fz = 0.0f;
+                ax += fx; ay += fy; az += fz;
+                bsx += fx; bsy += fy; bsz += fz;
+                ax = __shfl_sync(0xffffffffu, ax, nxt);
+                ay = __shfl_sync(0xffffffffu, ay, nxt);
+                az = __shfl_sync(0xffffffffu, az, nxt);
+            }
+        };
+        if (X != Y && (X + 1) * kBlock <= n)
+            sweep(std::true_type{});
+        else
+            sweep(std::false_type{});
+        __syncwarp();  // the row torques' shared-memory adds
+        // lane l holds row l's force sum (rows and columns beyond n hold 0)
+        const int sAl = X * kBlock + lane;
+        const float ima = rows[lane * kRowStrideT + 9];
+        const float rtx = rowtq[lane], rty = rowtq[kBlock + lane], rtz = rowtq[2 * kBlock + lane];
+        if (X == Y) {  // the same sphere: partners before it in slot order (row), after it (column)
+            const size_t o = (size_t)X * b.part_np + sAl;
+            part[o] = fmaf(ima, ax, -inv_mb * bsx);
+            part[o + pplane] = fmaf(ima, ay, -inv_mb * bsy);
+            part[o + 2 * pplane] = fmaf(ima, az, -inv_mb * bsz);
+            part[o + 3 * pplane] = rtx + ctx;
+            part[o + 4 * pplane] = rty + cty;
+            part[o + 5 * pplane] = rtz + ctz;
+        } else {
+            const size_t oa = (size_t)Y * b.part_np + sAl, ob = (size_t)X * b.part_np + sB;
+            part[oa] = ima * ax; part[oa + pplane] = ima * ay; part[oa + 2 * pplane] = ima * az;
+            part[oa + 3 * pplane] = rtx; part[oa + 4 * pplane] = rty; part[oa + 5 * pplane] = rtz;
+            part[ob] = -inv_mb * bsx; part[ob + pplane] = -inv_mb * bsy; part[ob + 2 * pplane] = -inv_mb * bsz;
+            part[ob + 3 * pplane] = ctx; part[ob + 4 * pplane] = cty; part[ob + 5 * pplane] = ctz;
+        }
+        __syncwarp();
+    }
+    if (WRITE) pe += -M.Ha / 6 * (f2d_bits(pe_far.s) + f2d_bits(pe_far.c));
+    return pe;
+}
+
+// The CTA's per-sphere totals from the tile partials (partner blocks in
+// ascending order, compensated sums), to acc and aacc in the caller's order.
+__device__ __forceinline__ void tile_totals(const Batch& b, int off, int n)
+{
+    const int nbk = (n + kBlock - 1) / kBlock;
+    const float* part = b.part + (size_t)blockIdx.x * b.part_cta;
+    const size_t pplane = (size_t)b.part_nb * b.part_np;
+    for (int p = threadIdx.x; p < n; p += blockDim.x) {
+        df::Sum tot[6] = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}};
+        for (int K = 0; K < nbk; ++K) {
+            const float* e = part + (size_t)K * b.part_np + p;
+#pragma unroll
+            for (int q = 0; q < 6; ++q) tot[q].add(e[q * pplane]);
+        }
+        const int g = b.perm[off + p];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            b.acc.c[c][g] = f2d_bits(tot[c].s) + f2d_bits(tot[c].c);
+            b.aacc.c[c][g] = f2d_bits(tot[3 + c].s) + f2d_bits(tot[3 + c].c);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(32 * kTileWarps) batch_mixed_tiles_kernel(const __grid_constant__ Batch b,
+                                                                           int first_step, int nsteps, int skip,
+                                                                           int do_init)
+{
+    __shared__ TileSmem ts;
+    __shared__ double sh[8][32];
+    __shared__ int s_next;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_next = atomicAdd(b.counter, 1);
+        __syncthreads();
+        const int k = s_next;
+        if (k >= b.ninst) return;
+        const int inst = b.order[k];
+        const int off = b.off[inst], n = b.cnt[inst];
+        Material M = b.mat;
+        M.u_s = b.u_s[inst];
+        const double dt = b.dt[inst], kin = b.kin[inst], kout = b.kout[inst];
+        double* recs = b.energy + (size_t)inst * b.nrec * 8;
+        if (do_init) {
+            drift(b, off, n, 0.0);
+            __syncthreads();
+            const double pe = tile_pass_mixed<true>(b, off, n, M, kin, kout, ts);
+            __syncthreads();
+            tile_totals(b, off, n);
+            __syncthreads();
+            kick(b, inst, off, n, 0.0, true, pe, recs, sh);
+            __syncthreads();
+        }
+        for (int q = 0; q < nsteps; ++q) {
+            const int step = first_step + q;
+            const bool write = skip > 0 && step % skip == 0;
+            drift(b, off, n, dt);
+            __syncthreads();
+            double pe = 0;
+            if (write)
+                pe = tile_pass_mixed<true>(b, off, n, M, kin, kout, ts);
+            else
+                tile_pass_mixed<false>(b, off, n, M, kin, kout, ts);
+            __syncthreads();
+            tile_totals(b, off, n);
+            __syncthreads();
+            const int r = write ? step / skip : 0;
+            kick(b, inst, off, n, dt, write, pe, recs + (size_t)(r < b.nrec ? r : b.nrec - 1) * 8, sh);
+            __syncthreads();
+        }
+    }
+}
+
 }  // namespace
 
 void launch_batch_mixed(const Batch& b, int tile, int threads, int blocks, int first_step, int nsteps, int skip,
                         int do_init, cudaStream_t st)
 {
     switch (tile) {
+        case 0: batch_mixed_tiles_kernel<<<blocks, threads, 0, st>>>(b, first_step, nsteps, skip, do_init); break;
         case 32: batch_mixed_kernel<32><<<blocks, threads, 0, st>>>(b, first_step, nsteps, skip, do_init); break;
         case 64: batch_mixed_kernel<64><<<blocks, threads, 0, st>>>(b, first_step, nsteps, skip, do_init); break;
         default: batch_mixed_kernel<128><<<blocks, threads, 0, st>>>(b, first_step, nsteps, skip, do_init); break;
@@ -275,6 +544,7 @@ int batch_mixed_max_blocks_per_sm(int tile, int threads)
 {
     int nb = 0;
     switch (tile) {
+        case 0: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_mixed_tiles_kernel, threads, 0); break;
         case 32: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_mixed_kernel<32>, threads, 0); break;
         case 64: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_mixed_kernel<64>, threads, 0); break;
         default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_mixed_kernel<128>, threads, 0); break;

@@ -74,6 +74,7 @@ def test_batch_shapes_agree_and_autotuner_picks_one():
     run = B.BatchRun(cols, "exact", steps=10, skip=5)
     tuned = run.autotune(sample_steps=2)
     assert tuned["tile"] in (32, 64, 128) and tuned["threads"] in (64, 128, 256)
+    assert len(tuned["times_ms"]) == 9  # the pair-tile pass is the mixed form's
     assert all(t > 0 for t in tuned["times_ms"].values())
     run.run(1, 10, do_init=True)   # the autotuner restored the initial state
     st = run.state()
@@ -81,10 +82,15 @@ def test_batch_shapes_agree_and_autotuner_picks_one():
         assert np.array_equal(st[k], results[0][k])
 
 
-def test_mixed_batch_tracks_exact_batch():
+@pytest.mark.parametrize("shape", [(64, 128), (0, 256), (0, 64)])
+def test_mixed_batch_tracks_exact_batch(shape):
+    """Both mixed pair passes: the per-sphere partner loop (j-tiles of 64)
+    and the pair-tile pass (tile 0: each pair once, Z-ordered 32-sphere
+    blocks, contacts in the reference's orientation)."""
     cols = _instances()
     ex = B.BatchRun(cols, "exact", steps=40, skip=10)
     mx = B.BatchRun(cols, "mixed", steps=40, skip=10)
+    mx.set_shape(*shape)
     ex.run(1, 40, True)
     mx.run(1, 40, True)
     se, sm = ex.state(), mx.state()
@@ -99,3 +105,13 @@ def test_mixed_batch_tracks_exact_batch():
         E = ee[i][:, 0] + ee[i][:, 1]
         Em = em[i][:, 0] + em[i][:, 1]
         assert np.abs(Em - E).max() <= tol_E * np.abs(E).max(), i
+
+
+def test_mixed_batch_autotuner_includes_pair_tiles():
+    cols = _instances()
+    run = B.BatchRun(cols, "mixed", steps=10, skip=5)
+    tuned = run.autotune(sample_steps=2)
+    assert len(tuned["times_ms"]) == 12 and all(t > 0 for t in tuned["times_ms"].values())
+    assert tuned["tile"] in (0, 32, 64, 128)
+    run.run(1, 10, do_init=True)
+    assert not run.status().any()
