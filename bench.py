@@ -379,7 +379,7 @@ def run_batched(args) -> dict:
     build_s = time.perf_counter() - t0
     steps = args.batch_steps
     run = B.BatchRun(cols, args.mode, steps=steps, skip=100)
-    tuned = run.autotune(sample_steps=2)
+    tuned = run.autotune(sample_steps=8)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     ev0.record()

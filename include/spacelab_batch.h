@@ -40,15 +40,17 @@ int sl_batch_upload(sl_batch* b, const double* pos, const double* vel, const dou
 /* Launch shape: j-tile size (32, 64, 128 spheres staged in shared memory)
  * and threads per instance (64, 128, 256 = the block size).  In the mixed
  * form tile 0 selects the pair-tile pass instead: every pair evaluated once,
- * in 32 x 32 blocks of Z-ordered spheres, with per-CTA partial sums. */
+ * in 32 x 32 blocks of Z-ordered spheres, with per-CTA partial sums; it also
+ * takes 512 threads. */
 int sl_batch_set_shape(sl_batch* b, int tile, int threads);
 int sl_batch_shape(const sl_batch* b, int* tile, int* threads, int* blocks);
 
 /* Autotuner: times every tile x threads candidate on sample_steps steps of
  * the whole batch (from a saved copy of the current state, restored
  * afterwards), keeps the fastest and returns it; times_ms (12 entries,
- * tile-major in the order 32, 64, 128, 0, may be NULL) gets each
- * candidate's time, -1 for tile 0 in the exact form. */
+ * tile-major in the order 32, 64, 128, 0, threads 64, 128, 256 -- for tile
+ * 0: 128, 256, 512 -- may be NULL) gets each candidate's time, -1 for tile 0
+ * in the exact form. */
 int sl_batch_autotune(sl_batch* b, int sample_steps, int* tile, int* threads, double* times_ms);
 
 /* One persistent launch: the initial force pass if do_init, then steps

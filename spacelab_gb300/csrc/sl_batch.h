@@ -35,7 +35,7 @@ struct Batch {
     // the radii's double-float lo parts, and the positions as double-float
     // hi (x, y, z) and lo (x, y, z), written by the drift
     float *f_Rlo, *f_pos[6];
-    float far_sq, series_sq;  // far-pair thresholds (far_thresholds in sl_pair_mixed.cuh)
+    float far_sq;  // far-pair threshold (far_threshold_sq in sl_pair_mixed.cuh)
     // mixed form, pair-tile pass (shape tile 0): per-CTA scratch of tile
     // partials, CTA c at part + c * part_cta, [6][part_nb][part_np] floats
     float* part;

@@ -30,6 +30,7 @@ size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 const int kTiles[4] = {32, 64, 128, 0};  // 0: the mixed form's pair-tile pass
 const int kThreads[3] = {64, 128, 256};
+const int kThreadsTiles[3] = {128, 256, 512};  // the pair-tile pass's candidates
 
 }  // namespace
 
@@ -295,7 +296,7 @@ int sl_batch_upload(sl_batch* h, const double* pos, const double* vel, const dou
     b.len_shift = ex - 1;
     double rmin = R[0];
     for (size_t i = 0; i < T; ++i) rmin = std::min(rmin, R[i]);
-    sl::far_thresholds(b.mat.h_min, rmin, b.far_sq, b.series_sq);
+    b.far_sq = sl::far_threshold_sq(b.mat.h_min, rmin);
     std::vector<double> tmp(T);
     const double* v3[3] = {pos, vel, w};
     sl::Vec3Soa* dv[3] = {&b.pos, &b.vel, &b.w};
@@ -330,8 +331,9 @@ int sl_batch_upload(sl_batch* h, const double* pos, const double* vel, const dou
 int sl_batch_set_shape(sl_batch* h, int tile, int threads)
 {
     if (!h) return sl_record_error(SL_ERR_ARG, "null batch");
-    if ((tile != 32 && tile != 64 && tile != 128 && tile != 0) || (threads != 64 && threads != 128 && threads != 256))
-        return sl_record_error(SL_ERR_ARG, "tile must be 32/64/128 (or 0) and threads 64/128/256");
+    const bool threads_ok = threads == 64 || threads == 128 || threads == 256 || (tile == 0 && threads == 512);
+    if ((tile != 32 && tile != 64 && tile != 128 && tile != 0) || !threads_ok)
+        return sl_record_error(SL_ERR_ARG, "tile must be 32/64/128 (or 0) and threads 64/128/256 (or 512 with tile 0)");
     if (tile == 0 && h->mode != SL_MODE_MIXED) return sl_record_error(SL_ERR_ARG, "tile 0 is the mixed form's");
     h->tile = tile;
     h->threads = threads;
@@ -355,16 +357,17 @@ int sl_batch_autotune(sl_batch* h, int sample_steps, int* tile, int* threads, do
                 continue;
             }
             if (int r = snapshot_copy(h, false)) return r;
+            const int thr = kTiles[ti] == 0 ? kThreadsTiles[hi] : kThreads[hi];
             // first launch compiles nothing but warms the caches; time the second
-            if (int r = launch_run(h, kTiles[ti], kThreads[hi], 1, 1, 0, 0)) return r;
+            if (int r = launch_run(h, kTiles[ti], thr, 1, 1, 0, 0)) return r;
             cudaEventRecord(e0, h->stream);
-            if (int r = launch_run(h, kTiles[ti], kThreads[hi], 2, sample_steps, 0, 0)) return r;
+            if (int r = launch_run(h, kTiles[ti], thr, 2, sample_steps, 0, 0)) return r;
             cudaEventRecord(e1, h->stream);
             cudaEventSynchronize(e1);
             float ms = 0;
             cudaEventElapsedTime(&ms, e0, e1);
             if (times_ms) times_ms[k] = ms;
-            if (ms < best) { best = ms; bt = kTiles[ti]; bth = kThreads[hi]; }
+            if (ms < best) { best = ms; bt = kTiles[ti]; bth = thr; }
         }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

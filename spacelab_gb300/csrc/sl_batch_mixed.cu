@@ -1,11 +1,11 @@
 // sl_batch_mixed.cu -- batched solver in the mixed-precision form: the same
 // persistent work-queue launch as sl_batch.cu, with the pair pass of the
-// mixed form: far pairs entirely in FP32 (no square root), near pairs with
+// mixed form: far pairs entirely in FP32 (no square root), close pairs with
 // double-float (sl_df.cuh) displacement, |r|^2 and squared gap from the
 // double-float positions the drift writes; FP32 forces and torques; FP32
 // sums per j-tile joined in compensated per-sphere totals, converted to
-// FP64; FP64 kin/kout test and write-step potential energy of near pairs
-// from the FP64 positions (far pairs: the FP32 series of vdw_bracket_far).
+// FP64; FP64 kin/kout test and write-step potential energy of close pairs
+// from the FP64 positions (far pairs: the FP32 series of vdw_bracket).
 // The non-contact pair path issues no FP64 instruction.
 #include "sl_batch.h"
 #include "sl_batch_common.cuh"
@@ -161,15 +161,7 @@ __device__ double pair_pass_mixed(const Batch& b, int off, int n, const Material
                     fx = use ? fr * rx : 0.0f;
                     fy = use ? fr * ry : 0.0f;
                     fz = use ? fr * rz : 0.0f;
-                    if (WRITE && use && i > j) {
-                        if (!(d2 < b.series_sq * sum2)) {
-                            pe_far.add(vdw_bracket_far(T, Ri, Rj));
-                        } else {  // outside the series' range: FP64, as the close pairs
-                            const double d2_64 = fp64_d2(b, off + i, off + j), sum64 = b.R[off + i] + b.R[off + j];
-                            pe += pair_pe_fp64(M, b.R[off + i], b.R[off + j], fma(sum64, sum64, -d2_64), d2_64, false,
-                                               0.0);
-                        }
-                    }
+                    if (WRITE && use && i > j) pe_far.add(vdw_bracket(d2, Ri, Rj));
                     return valid && close;
                 };
                 const int jend = min(TILE, n - jbase);
@@ -274,7 +266,7 @@ __global__ void __launch_bounds__(256) batch_mixed_kernel(const __grid_constant_
 // (one lane per row in a step, the steps in program order, so the order is
 // fixed), a column sphere's in a register.
 constexpr int kRowStrideT = 12;  // floats per row sphere: hi xyz R | lo xyz cR3 | Rlo 1/m 1/moi index
-constexpr int kTileWarps = 8;
+constexpr int kTileWarps = 16;  // up to 512 threads: a large instance can have a whole SM
 
 struct TileSmem {
     float rows[kTileWarps][kBlock * kRowStrideT];
@@ -407,16 +399,7 @@ __device__ double tile_pass_mixed(const Batch& b, int off, int n, const Material
                 float fx = fr * rx, fy = fr * ry, fz = fr * rz;
                 const bool close = d2 < b.far_sq * sum2;
                 if (valid && close) close_pair(r, fx, fy, fz);
-                if (WRITE && valid && !close) {
-                    if (!(d2 < b.series_sq * sum2)) {
-                        pe_far.add(vdw_bracket_far(T, Ras, Rbs));
-                    } else {  // outside the series' range: FP64, as the close pairs
-                        const int iA = __float_as_int(rows[r * kRowStrideT + 11]);
-                        const double d2_64 = fp64_d2(b, off + iA, off + iB), sum64 = b.R[off + iA] + b.R[off + iB];
-                        pe += pair_pe_fp64(M, b.R[off + iA], b.R[off + iB], fma(sum64, sum64, -d2_64), d2_64, false,
-                                           0.0);
-                    }
-                }
+                if (WRITE && valid && !close) pe_far.add(vdw_bracket(d2, Ras, Rbs));
                 if (!FULL && !valid) fx = fy = fz = 0.0f;
                 ax += fx; ay += fy; az += fz;
                 bsx += fx; bsy += fy; bsz += fz;

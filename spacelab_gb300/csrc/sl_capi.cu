@@ -350,7 +350,7 @@ int sl_upload(sl_handle* h, const double* pos, const double* vel, const double* 
     int ex = 0;
     std::frexp(rmax, &ex);
     h->sys.len_shift = ex - 1;
-    sl::far_thresholds(h->sys.mat.h_min, rmin, h->sys.far_sq, h->sys.series_sq);
+    h->sys.far_sq = sl::far_threshold_sq(h->sys.mat.h_min, rmin);
     // padded spheres get R = m = moi = 1 (they are never paired)
     const double* src[3] = {R, m, moi};
     double* dst[3] = {h->sys.R, h->sys.m, h->sys.moi};

@@ -71,9 +71,9 @@ struct System {
     // mixed form: the pair kernel's tile counter (zeroed by the drift kernel)
     int* tile_counter;
     int len_shift;
-    // mixed form: squared separation factors of the far-pair force and
-    // potential paths (far_thresholds in sl_pair_mixed.cuh)
-    float far_sq, series_sq;
+    // mixed form: squared separation factor of the far-pair paths
+    // (far_threshold_sq in sl_pair_mixed.cuh)
+    float far_sq;
 };
 
 // Operands of a pair's contact branch beyond positions and radii (the

@@ -28,14 +28,13 @@ __device__ __forceinline__ float vdw_shape(float h, float Ra, float Rb)
 // ~1.5 bits of |r|^2's precision, and the force comes out within ~2e-6 of the
 // FP64 formula (measured over separations 1.25-4 radii sums, split positions
 // up to 60 radii from the origin).  Closer pairs -- contacts and small gaps --
-// take the double-float geometry.  The far-pair potential series needs
-// |r| >= 2 (R_A + R_B) as well: series_sq = max(4, far_sq).
-inline void far_thresholds(double h_min, double r_min, float& far_sq, float& series_sq)
+// take the double-float geometry.  The far pairs' write-step potential is
+// the series of vdw_bracket, valid over the same range.
+inline float far_threshold_sq(double h_min, double r_min)
 {
     double far = 1.0 + h_min / (2.0 * r_min);
     if (far < 1.25) far = 1.25;
-    far_sq = (float)(far * far);
-    series_sq = far_sq > 4.0f ? far_sq : 4.0f;
+    return (float)(far * far);
 }
 
 // Approximate FP32 reciprocal (one MUFU instruction, relative error below
@@ -49,29 +48,32 @@ __device__ __forceinline__ float rcp_approx(float x)
 
 // The vdW potential's bracket 2RaRb/P + 2RaRb/Q + ln(P/Q), P = z^2 - (Ra+Rb)^2,
 // Q = z^2 - (Ra-Rb)^2 (ColliderSingleCore.cpp:228-240; U = -Ha/6 times it),
-// for a pair at centre distance z >= 2 (Ra + Rb), from Q in scaled lengths.
-// With u = 4 Ra Rb / Q (P/Q = 1 - u) the bracket is
-// u/(2(1-u)) + u/2 + ln(1-u) = sum_{k>=3} (k-2)/(2k) u^k: its O(u) and
-// O(u^2) parts cancel exactly, which the closed form resolves only in FP64.
-// Here u <= 1/4, so the terms up to k = 15 leave a relative truncation
-// error below 5e-8, and FP32 Horner evaluation suffices.
-__device__ __forceinline__ float vdw_bracket_far(float Q, float Ra, float Rb)
+// for a pair at centre distance z >= far (Ra + Rb), from d2 = z^2 in scaled
+// lengths.  Its O(z^-2) and O(z^-4) parts cancel exactly, which the closed
+// form resolves only in FP64.  With w = 2 Ra Rb / (z^2 - Ra^2 - Rb^2)
+// (u = 4 Ra Rb / Q = 2w / (1 + w), so 1 - u = (1 - w) / (1 + w)) the bracket
+// is 2w/(1 - w^2) - 2 atanh(w) = sum_{j>=1} 4j/(2j+1) w^(2j+1), all terms
+// positive.  At z >= 1.25 (Ra + Rb), w <= 0.47 and w^2 <= 0.22: twelve
+// terms by Horner in FP32 leave a relative truncation error below 2e-8
+// (checked against 40-digit arithmetic); the FP32 rounding of z^2 bounds the
+// result to ~7e-7 relative.
+__device__ __forceinline__ float vdw_bracket(float d2, float Ra, float Rb)
 {
-    const float u = (4.0f * Ra * Rb) * rcp_approx(Q);
-    float p = 13.0f / 30.0f;                 // k = 15
-    p = fmaf(p, u, 3.0f / 7.0f);             // 14
-    p = fmaf(p, u, 11.0f / 26.0f);           // 13
-    p = fmaf(p, u, 5.0f / 12.0f);            // 12
-    p = fmaf(p, u, 9.0f / 22.0f);            // 11
-    p = fmaf(p, u, 2.0f / 5.0f);             // 10
-    p = fmaf(p, u, 7.0f / 18.0f);            // 9
-    p = fmaf(p, u, 3.0f / 8.0f);             // 8
-    p = fmaf(p, u, 5.0f / 14.0f);            // 7
-    p = fmaf(p, u, 1.0f / 3.0f);             // 6
-    p = fmaf(p, u, 3.0f / 10.0f);            // 5
-    p = fmaf(p, u, 1.0f / 4.0f);             // 4
-    p = fmaf(p, u, 1.0f / 6.0f);             // 3
-    return (u * u) * (u * p);
+    const float w = (2.0f * Ra * Rb) * rcp_approx(fmaf(-Ra, Ra, fmaf(-Rb, Rb, d2)));
+    const float x = w * w;
+    float p = 48.0f / 25.0f;                 // j = 12: 4j/(2j+1)
+    p = fmaf(p, x, 44.0f / 23.0f);           // 11
+    p = fmaf(p, x, 40.0f / 21.0f);           // 10
+    p = fmaf(p, x, 36.0f / 19.0f);           // 9
+    p = fmaf(p, x, 32.0f / 17.0f);           // 8
+    p = fmaf(p, x, 28.0f / 15.0f);           // 7
+    p = fmaf(p, x, 24.0f / 13.0f);           // 6
+    p = fmaf(p, x, 20.0f / 11.0f);           // 5
+    p = fmaf(p, x, 16.0f / 9.0f);            // 4
+    p = fmaf(p, x, 12.0f / 7.0f);            // 3
+    p = fmaf(p, x, 8.0f / 5.0f);             // 2
+    p = fmaf(p, x, 4.0f / 3.0f);             // 1
+    return (w * x) * p;
 }
 
 struct ContactF {

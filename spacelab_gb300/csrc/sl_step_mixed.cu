@@ -4,8 +4,8 @@
 //   * FP64: positions and the whole integration (drift_kernel, shared with
 //     the exact form; pass 3 in mixed_finish_kernel), the previous-step
 //     distance test that chooses kin or kout, the write-step potential
-//     energy of near pairs and the energy totals (far pairs' vdW potential
-//     comes from a cancellation-free series in FP32, vdw_bracket_far);
+//     energy of close pairs and the energy totals (far pairs' vdW potential
+//     comes from a cancellation-free series in FP32, vdw_bracket);
 //   * double-float (hi + lo FP32 pairs, ~48 significant bits, sl_df.cuh):
 //     for pairs closer than 1.25 times the sum of their radii, the subtraction
 //     r = pos[B] - pos[A] from double-float copies of the scaled positions,
@@ -86,7 +86,7 @@ __global__ void __launch_bounds__(32 * kPairWarps, kPairCtasPerSm) mixed_pair_ke
     const float hmin_s = (float)s.mat.h_min / L;
     const float c_vdw = (float)(s.mat.Ha / 6 * 64) / L;   // dyn per unit vdw_shape
     const int nxt = (lane + 1) & (kBlock - 1);
-    // write steps: near pairs out of contact whose FP64 potential is pending.
+    // write steps: close pairs out of contact whose FP64 potential is pending.
     // Their FP64 evaluation runs with every lane busy (the FP64 pipe takes a
     // warp instruction per ~64 cycles however few lanes are active)
     __shared__ int2 queue_all[WRITE ? kPairWarps : 1][WRITE ? 2 * kBlock : 1];
@@ -110,7 +110,7 @@ __global__ void __launch_bounds__(32 * kPairWarps, kPairCtasPerSm) mixed_pair_ke
     // Tiles: a first round in warp order, then, on plain steps, whichever
     // warp is free takes the next tile from a counter that the drift kernel
     // zeroes (the last round of a static stride leaves SMs idle); write
-    // steps keep the static stride, so that their near-pair queues, and so
+    // steps keep the static stride, so that their close-pair queues, and so
     // the potential energy's rounding, repeat run to run.
     long long t = (long long)blockIdx.x * kPairWarps + wib;
     for (; t < s.ntiles;) {
@@ -167,8 +167,8 @@ __global__ void __launch_bounds__(32 * kPairWarps, kPairCtasPerSm) mixed_pair_ke
                 const float fr = (q1.w * Rb3) * rcp_approx(P * P);  // |F| / |r|
                 float fx = fr * rx, fy = fr * ry, fz = fr * rz;
                 bool contact = false;
-                const bool nearp = d2 < s.series_sq * sum2;  // outside the far-pair potential series' range
-                if (valid && d2 < s.far_sq * sum2) {
+                const bool closep = d2 < s.far_sq * sum2;
+                if (valid && closep) {
                     // close pair: double-float (~48 bits, FP32 pipe) subtraction,
                     // |r|^2 and squared gap g = (R_A + R_B)^2 - |r|^2
                     const int A = X * kBlock + r;
@@ -209,9 +209,9 @@ __global__ void __launch_bounds__(32 * kPairWarps, kPairCtasPerSm) mixed_pair_ke
                     }
                 }
                 if (WRITE) {  // write steps only
-                    if (valid && !nearp) pe_far.add(vdw_bracket_far(T, Ras, Rbs));
-                    // near pairs out of contact: queued, evaluated 32 at a time
-                    const bool need = valid && nearp && !contact;
+                    if (valid && !closep) pe_far.add(vdw_bracket(d2, Ras, Rbs));
+                    // close pairs out of contact: queued, evaluated 32 at a time
+                    const bool need = valid && closep && !contact;
                     const uint32_t m = __ballot_sync(0xffffffffu, need);
                     if (m) {
                         if (need) q[qn + __popc(m & ((1u << lane) - 1u))] = make_int2(X * kBlock + r, B);
