@@ -487,7 +487,7 @@ def main(argv=None) -> int:
     ap.add_argument("--baseline-instances", type=int, default=16)
     ap.add_argument("--surrogate-study", action="store_true",
                     help="instead of the benchmark: train the surrogate ensemble and screen a sweep")
-    ap.add_argument("--train-collisions", type=int, default=8000)
+    ap.add_argument("--train-collisions", type=int, default=50000)
     ap.add_argument("--sweep-points", type=int, default=100000)
     ap.add_argument("--study-steps", type=int, default=4000)
     ap.add_argument("--epochs", type=int, default=150)
