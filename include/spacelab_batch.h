@@ -38,10 +38,12 @@ int sl_batch_upload(sl_batch* b, const double* pos, const double* vel, const dou
                     const double* u_s);
 
 /* Launch shape: j-tile size (32, 64, 128 spheres staged in shared memory)
- * and threads per instance (64, 128, 256 = the block size).  In the mixed
- * form tile 0 selects the pair-tile pass instead: every pair evaluated once,
- * in 32 x 32 blocks of Z-ordered spheres, with per-CTA partial sums; it also
- * takes 512 threads. */
+ * and threads per instance (64, 128, 256 = the block size).  Tile 0
+ * selects the pair-tile pass instead, every pair evaluated once in 32 x 32
+ * blocks: in the mixed form over Z-ordered spheres with per-CTA partial sums
+ * (also at 512 threads); in the exact form with per-CTA pair-term buffers and
+ * ordered row sums, bit-identical to the other shapes (SL_ERR_UNSUPPORTED
+ * where the largest instance makes those buffers too big). */
 int sl_batch_set_shape(sl_batch* b, int tile, int threads);
 int sl_batch_shape(const sl_batch* b, int* tile, int* threads, int* blocks);
 
@@ -49,8 +51,8 @@ int sl_batch_shape(const sl_batch* b, int* tile, int* threads, int* blocks);
  * the whole batch (from a saved copy of the current state, restored
  * afterwards), keeps the fastest and returns it; times_ms (12 entries,
  * tile-major in the order 32, 64, 128, 0, threads 64, 128, 256 -- for tile
- * 0: 128, 256, 512 -- may be NULL) gets each candidate's time, -1 for tile 0
- * in the exact form. */
+ * 0 in the mixed form: 128, 256, 512 -- may be NULL) gets each candidate's
+ * time, -1 where tile 0 is unavailable. */
 int sl_batch_autotune(sl_batch* b, int sample_steps, int* tile, int* threads, double* times_ms);
 
 /* One persistent launch: the initial force pass if do_init, then steps

@@ -21,6 +21,7 @@
 #include "sl_batch_common.cuh"
 #include "sl_fp64_exact.cuh"
 #include "sl_pair_exact.cuh"
+#include "sl_tile_exact.cuh"
 
 namespace sl {
 
@@ -169,6 +170,169 @@ __global__ void __launch_bounds__(256) batch_exact_kernel(const __grid_constant_
     }
 }
 
+// ---------------------------------------------------------------------------
+// Pair-tile pass (shape tile 0): every pair once, as the single-system step
+// does it.  The CTA's warps take the instance's 32 x 32 block tiles and run
+// the single system's tile routine (tile_pairs, sl_tile_exact.cuh) on a
+// System view of the instance whose pair-term, torque and contact buffers are
+// the CTA's scratch; then thread (c, i) adds row i of the pair terms in
+// ascending partner order and its contact torques likewise -- the
+// reference's order, so the result stays bit-identical -- and the half-kick
+// follows.  This evaluates each pair once where the per-sphere loop does it
+// twice, at the price of the row sums' dependent FP64 adds.
+__device__ void make_view(System& v, const Batch& b, int inst, int off, int n)
+{
+    v = System{};
+    v.n = n;
+    v.nb = (n + kBlock - 1) / kBlock;
+    v.npad = b.x_np;  // the scratch's row stride
+    v.ntiles = (long long)v.nb * (v.nb + 1) / 2;
+    const Vec3Soa* src[8] = {&b.pos, &b.prev, &b.vel, &b.velh, &b.w, &b.wh, &b.acc, &b.aacc};
+    Vec3Soa* dst[8] = {&v.pos, &v.prev, &v.vel, &v.velh, &v.w, &v.wh, &v.acc, &v.aacc};
+    for (int k = 0; k < 8; ++k)
+        for (int c = 0; c < 3; ++c) dst[k]->c[c] = src[k]->c[c] + off;
+    v.R = b.R + off; v.m = b.m + off; v.moi = b.moi + off;
+    v.twoR = b.twoR + off; v.fourR = b.fourR + off; v.cR3 = b.cR3 + off;
+    v.rm = b.rm + off; v.inv_moi = b.inv_moi + off;
+    v.pairbuf = b.xpair + (size_t)blockIdx.x * b.xpair_cta;
+    v.torqbuf = b.xtorq + (size_t)blockIdx.x * b.xpair_cta;
+    v.cmask = b.xmask + (size_t)blockIdx.x * b.xmask_cta;
+    v.sc = b.isc + inst;
+    v.mat = b.mat;
+    v.mat.u_s = b.u_s[inst];
+}
+
+template <bool WRITE>
+__device__ double exact_tile_pass(const System& s, ABlock* blocks)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    ABlock& ab = blocks[warp];
+    const int n = s.n;
+    const double Ha = s.mat.Ha;
+    const long long h_min_bits = __double_as_longlong(s.mat.h_min);  // h_min > 0
+    double pe = 0;
+    for (long long t = warp; t < s.ntiles; t += nwarps) {
+        int X, Y;
+        tile_coords(t, X, Y);
+        {
+            const int i = min(X * kBlock + lane, n - 1);  // padding rows repeat the last sphere (never paired)
+            ab.x[lane] = s.pos.c[0][i]; ab.y[lane] = s.pos.c[1][i]; ab.z[lane] = s.pos.c[2][i];
+            ab.R[lane] = s.R[i]; ab.twoR[lane] = s.twoR[i]; ab.fourR[lane] = s.fourR[i];
+            ab.cR3[lane] = s.cR3[i]; ab.m[lane] = s.m[i]; ab.rm[lane] = s.rm[i];
+        }
+        __syncwarp();
+        const int B = Y * kBlock + lane;
+        const bool bvalid = B < n;
+        const int Bc = min(B, n - 1);
+        const double bx = s.pos.c[0][Bc], by = s.pos.c[1][Bc], bz = s.pos.c[2][Bc];
+        const double Rb = s.R[Bc], twoRb = s.twoR[Bc], mb = s.m[Bc];
+        const unsigned long long rmb = s.rm[Bc];
+        const double R0 = ab.R[0];
+        const bool uni = __all_sync(0xffffffffu, ab.R[lane] == R0 && Rb == R0);
+        const double twoR0 = ab.twoR[0], sum0 = R0 + R0, c40 = ab.fourR[0] * R0;
+        const double P0 = ab.cR3[0] * R0 * R0 * R0;
+        const int a_end = min(kBlock, n - X * kBlock);
+        uint32_t rowbits = 0, colbits = 0;
+        double* rowA = s.pairbuf + (size_t)(X * kBlock) * s.npad + B;  // + a*npad: term for A
+        double* rowB = s.pairbuf + (size_t)B * s.npad + X * kBlock;    // + a: term for B
+        const TileUniform tu{R0, twoR0, sum0, c40, P0};
+        if (uni)
+            tile_pairs<WRITE, true>(s, ab, X, Y, lane, a_end, bx, by, bz, Rb, twoRb, mb, rmb, bvalid, tu, h_min_bits,
+                                    Ha, rowA, rowB, pe, rowbits, colbits);
+        else
+            tile_pairs<WRITE, false>(s, ab, X, Y, lane, a_end, bx, by, bz, Rb, twoRb, mb, rmb, bvalid, tu, h_min_bits,
+                                     Ha, rowA, rowB, pe, rowbits, colbits);
+        if (X == Y) {
+            s.cmask[(size_t)(X * kBlock + lane) * s.nb + X] = rowbits | colbits;
+        } else {
+            s.cmask[(size_t)(X * kBlock + lane) * s.nb + Y] = rowbits;
+            s.cmask[(size_t)(Y * kBlock + lane) * s.nb + X] = colbits;
+        }
+        __syncwarp();
+    }
+    return pe;
+}
+
+// Thread (c, i): acc_c[i] and aacc_c[i] in the reference's order
+// (ColliderSingleCore.cpp:100-103, 249-250): partners j < i, then j > i.
+__device__ void exact_row_sums(const System& s)
+{
+    const int n = s.n;
+    const size_t plane = (size_t)s.npad * s.npad;
+    for (int t = threadIdx.x; t < 3 * n; t += blockDim.x) {
+        const int c = t / n, i = t - c * n;
+        const double* row = s.pairbuf + c * plane + (size_t)i * s.npad;
+        double acc = 0;
+        for (int j = 0; j < i; ++j) acc += row[j];
+        for (int j = i + 1; j < n; ++j) acc += row[j];
+        const double* trow = s.torqbuf + c * plane + (size_t)i * s.npad;
+        const uint32_t* mrow = s.cmask + (size_t)i * s.nb;
+        double aacc = 0;
+        for (int Y = 0; Y < s.nb; ++Y) {
+            uint32_t wd = mrow[Y];
+            while (wd) {
+                const int j = Y * kBlock + __ffs(wd) - 1;
+                wd &= wd - 1;
+                aacc += trow[j];
+            }
+        }
+        s.acc.c[c][i] = acc;
+        s.aacc.c[c][i] = aacc;
+    }
+}
+
+constexpr int kExactTileWarps = 8;
+
+__global__ void __launch_bounds__(32 * kExactTileWarps) batch_exact_tiles_kernel(const __grid_constant__ Batch b,
+                                                                                int first_step, int nsteps, int skip,
+                                                                                int do_init)
+{
+    __shared__ ABlock blocks[kExactTileWarps];
+    __shared__ System sv;
+    __shared__ double sh[8][32];
+    __shared__ int s_next;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_next = atomicAdd(b.counter, 1);
+        __syncthreads();
+        const int k = s_next;
+        if (k >= b.ninst) return;
+        const int inst = b.order[k];
+        const int off = b.off[inst], n = b.cnt[inst];
+        const double dt = b.dt[inst];
+        double* recs = b.energy + (size_t)inst * b.nrec * 8;
+        if (threadIdx.x == 0) make_view(sv, b, inst, off, n);
+        __syncthreads();
+        if (do_init) {
+            drift(b, off, n, 0.0);
+            __syncthreads();
+            const double pe = exact_tile_pass<true>(sv, blocks);
+            __syncthreads();
+            exact_row_sums(sv);
+            __syncthreads();
+            kick(b, inst, off, n, 0.0, true, pe, recs, sh);
+            __syncthreads();
+        }
+        for (int q = 0; q < nsteps; ++q) {
+            const int step = first_step + q;
+            const bool write = skip > 0 && step % skip == 0;
+            drift(b, off, n, dt);
+            __syncthreads();
+            double pe = 0;
+            if (write)
+                pe = exact_tile_pass<true>(sv, blocks);
+            else
+                exact_tile_pass<false>(sv, blocks);
+            __syncthreads();
+            exact_row_sums(sv);
+            __syncthreads();
+            const int r = write ? step / skip : 0;
+            kick(b, inst, off, n, dt, write, pe, recs + (size_t)(r < b.nrec ? r : b.nrec - 1) * 8, sh);
+            __syncthreads();
+        }
+    }
+}
+
 __global__ void batch_derive_kernel(const __grid_constant__ Batch b)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -201,6 +365,7 @@ void launch_batch_exact(const Batch& b, int tile, int threads, int blocks, int f
                         int do_init, cudaStream_t st)
 {
     switch (tile) {
+        case 0: batch_exact_tiles_kernel<<<blocks, threads, 0, st>>>(b, first_step, nsteps, skip, do_init); break;
         case 32: batch_exact_kernel<32><<<blocks, threads, 0, st>>>(b, first_step, nsteps, skip, do_init); break;
         case 64: batch_exact_kernel<64><<<blocks, threads, 0, st>>>(b, first_step, nsteps, skip, do_init); break;
         default: batch_exact_kernel<128><<<blocks, threads, 0, st>>>(b, first_step, nsteps, skip, do_init); break;
@@ -212,6 +377,7 @@ int batch_max_blocks_per_sm(int tile, int threads, bool mixed)
     if (mixed) return batch_mixed_max_blocks_per_sm(tile, threads);
     int nb = 0;
     switch (tile) {
+        case 0: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_exact_tiles_kernel, threads, 0); break;
         case 32: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_exact_kernel<32>, threads, 0); break;
         case 64: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_exact_kernel<64>, threads, 0); break;
         default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_exact_kernel<128>, threads, 0); break;

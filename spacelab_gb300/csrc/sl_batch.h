@@ -40,7 +40,16 @@ struct Batch {
     // partials, CTA c at part + c * part_cta, [6][part_nb][part_np] floats
     float* part;
     size_t part_cta;
-    int part_nb, part_np, part_ctas;
+    int part_nb, part_np, part_ctas;  // part_ctas: CTAs the pair-tile scratch exists for (either form)
+    // exact form, pair-tile pass (shape tile 0): per-CTA pair-term and torque
+    // buffers [3][x_np][x_np] doubles and contact words [x_np][x_nb], the
+    // single-system layout at a fixed stride; NULL where the largest
+    // instance makes them too big
+    double *xpair, *xtorq;
+    uint32_t* xmask;
+    size_t xpair_cta, xmask_cta;
+    int x_np, x_nb;
+    Scalars* isc;  // per-instance dt, kin, kout as one record (the exact tile pass's System view)
     int len_shift;
     Material mat;         // G, Ha, u_r, h_min shared; u_s per instance
     double* energy;       // [ninst][nrec][8]

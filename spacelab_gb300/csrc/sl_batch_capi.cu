@@ -30,7 +30,10 @@ size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 const int kTiles[4] = {32, 64, 128, 0};  // 0: the mixed form's pair-tile pass
 const int kThreads[3] = {64, 128, 256};
-const int kThreadsTiles[3] = {128, 256, 512};  // the pair-tile pass's candidates
+const int kThreadsTiles[3] = {128, 256, 512};  // the mixed pair-tile pass's candidates
+// device memory the exact pair-tile pass's per-CTA buffers may take: at
+// most this, and at most a third of the free memory at creation
+constexpr size_t kExactTileScratchBytes = size_t(48) << 30;
 
 }  // namespace
 
@@ -211,6 +214,30 @@ int sl_batch_create(int ninst, const int* counts, const sl_material* mat, int mo
     b.part_cta = 6 * (size_t)b.part_nb * b.part_np;
     b.part_ctas = h->num_sms * sl::kTileCtasPerSm;
     const size_t o_part = take(mode == SL_MODE_MIXED ? b.part_cta * b.part_ctas * sizeof(float) : 0);
+    // exact: the pair-tile pass's per-CTA pair terms, torques and contact
+    // words at the largest instance's padded size, where that fits the
+    // budget for at least one CTA per SM
+    b.x_nb = b.part_nb;
+    b.x_np = b.part_np;
+    b.xpair_cta = 3 * (size_t)b.x_np * b.x_np;
+    b.xmask_cta = (size_t)b.x_np * b.x_nb;
+    size_t o_xpair = 0, o_xtorq = 0, o_xmask = 0;
+    bool exact_tiles = false;
+    if (mode == SL_MODE_EXACT) {
+        const size_t per_cta = 2 * b.xpair_cta * sizeof(double) + b.xmask_cta * sizeof(uint32_t);
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) free_b = 0;
+        const long long fit = (long long)(std::min(kExactTileScratchBytes, free_b / 3) / per_cta);
+        const long long ctas = std::min<long long>((long long)h->num_sms * sl::kTileCtasPerSm, fit);
+        if (ctas >= h->num_sms) {
+            exact_tiles = true;
+            b.part_ctas = (int)ctas;
+            o_xpair = take(b.xpair_cta * ctas * sizeof(double));
+            o_xtorq = take(b.xpair_cta * ctas * sizeof(double));
+            o_xmask = take(b.xmask_cta * ctas * sizeof(uint32_t));
+        }
+    }
+    const size_t o_isc = take((size_t)ninst * sizeof(sl::Scalars));
     h->arena_bytes = off;
     if (cudaMalloc(&h->arena, off) != cudaSuccess) {
         sl_batch_destroy(h);
@@ -241,6 +268,12 @@ int sl_batch_create(int ninst, const int* counts, const sl_material* mat, int mo
     double* par = reinterpret_cast<double*>(base + o_par);
     b.dt = par; b.kin = par + ninst; b.kout = par + 2 * ninst; b.u_s = par + 3 * ninst;
     b.energy = reinterpret_cast<double*>(base + o_en);
+    if (exact_tiles) {
+        b.xpair = reinterpret_cast<double*>(base + o_xpair);
+        b.xtorq = reinterpret_cast<double*>(base + o_xtorq);
+        b.xmask = reinterpret_cast<uint32_t*>(base + o_xmask);
+    }
+    b.isc = reinterpret_cast<sl::Scalars*>(base + o_isc);
     b.status = reinterpret_cast<unsigned*>(base + o_st);
     h->snapshot = reinterpret_cast<double*>(base + o_snap);
     // largest instances first: the work queue then balances like LPT scheduling
@@ -316,6 +349,9 @@ int sl_batch_upload(sl_batch* h, const double* pos, const double* vel, const dou
     double* dpar = const_cast<double*>(b.dt);
     for (int k = 0; k < 4; ++k)
         SLB_CUDA(cudaMemcpy(dpar + (size_t)k * b.ninst, par[k], b.ninst * sizeof(double), cudaMemcpyHostToDevice));
+    std::vector<sl::Scalars> isc(b.ninst);
+    for (int i = 0; i < b.ninst; ++i) isc[i] = sl::Scalars{dt[i], kin[i], kout[i]};
+    SLB_CUDA(cudaMemcpy(b.isc, isc.data(), b.ninst * sizeof(sl::Scalars), cudaMemcpyHostToDevice));
     if (b.perm) {
         const std::vector<int> perm = zorder_perm(h->offsets, h->counts, pos);
         SLB_CUDA(cudaMemcpy(const_cast<int*>(b.perm), perm.data(), T * sizeof(int), cudaMemcpyHostToDevice));
@@ -331,10 +367,13 @@ int sl_batch_upload(sl_batch* h, const double* pos, const double* vel, const dou
 int sl_batch_set_shape(sl_batch* h, int tile, int threads)
 {
     if (!h) return sl_record_error(SL_ERR_ARG, "null batch");
-    const bool threads_ok = threads == 64 || threads == 128 || threads == 256 || (tile == 0 && threads == 512);
+    const bool mixed = h->mode == SL_MODE_MIXED;
+    const bool threads_ok = threads == 64 || threads == 128 || threads == 256 || (tile == 0 && mixed && threads == 512);
     if ((tile != 32 && tile != 64 && tile != 128 && tile != 0) || !threads_ok)
-        return sl_record_error(SL_ERR_ARG, "tile must be 32/64/128 (or 0) and threads 64/128/256 (or 512 with tile 0)");
-    if (tile == 0 && h->mode != SL_MODE_MIXED) return sl_record_error(SL_ERR_ARG, "tile 0 is the mixed form's");
+        return sl_record_error(SL_ERR_ARG,
+                               "tile must be 32/64/128 (or 0) and threads 64/128/256 (or 512 with tile 0, mixed)");
+    if (tile == 0 && !mixed && !h->b.xpair)
+        return sl_record_error(SL_ERR_UNSUPPORTED, "the exact pair-tile pass's buffers do not fit for this batch");
     h->tile = tile;
     h->threads = threads;
     return SL_OK;
@@ -352,12 +391,13 @@ int sl_batch_autotune(sl_batch* h, int sample_steps, int* tile, int* threads, do
     int bt = h->tile, bth = h->threads, k = 0;
     for (int ti = 0; ti < 4; ++ti)
         for (int hi = 0; hi < 3; ++hi, ++k) {
-            if (kTiles[ti] == 0 && h->mode != SL_MODE_MIXED) {
+            const bool mixed = h->mode == SL_MODE_MIXED;
+            if (kTiles[ti] == 0 && !mixed && !h->b.xpair) {
                 if (times_ms) times_ms[k] = -1.0;
                 continue;
             }
             if (int r = snapshot_copy(h, false)) return r;
-            const int thr = kTiles[ti] == 0 ? kThreadsTiles[hi] : kThreads[hi];
+            const int thr = kTiles[ti] == 0 && mixed ? kThreadsTiles[hi] : kThreads[hi];
             // first launch compiles nothing but warms the caches; time the second
             if (int r = launch_run(h, kTiles[ti], thr, 1, 1, 0, 0)) return r;
             cudaEventRecord(e0, h->stream);

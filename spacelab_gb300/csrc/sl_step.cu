@@ -29,6 +29,7 @@
 #include "sl_kernels.h"
 #include "sl_fp64_exact.cuh"
 #include "sl_pair_exact.cuh"
+#include "sl_tile_exact.cuh"
 
 #include <cstdio>
 
@@ -64,95 +65,6 @@ __global__ void __launch_bounds__(kDriftThreads) drift_kernel(const __grid_const
 }
 
 // ---------------------------------------------------------------- pass 2 --
-// Per-warp staging of the A block (lane l holds sphere X*32+l).
-struct ABlock {
-    double x[kBlock], y[kBlock], z[kBlock], R[kBlock], twoR[kBlock], fourR[kBlock], cR3[kBlock], m[kBlock];
-    unsigned long long rm[kBlock];
-};
-
-// Equal radii across a tile (monodisperse clusters): the sum of radii and
-// the vdW coefficient's radius products are the same for every pair of the
-// tile and are formed once (vdw_coef_uniform).
-struct TileUniform {
-    double R0, twoR0, sum0, c40, P0;
-};
-
-// The pairs of one tile (X, Y) for lane = sphere B: terms to pairbuf and
-// torqbuf, contact bits to rowbits/colbits, PE (write steps) to pe.
-template <bool WRITE, bool UNI>
-__device__ __forceinline__ void tile_pairs(const System& s, const ABlock& ab, int X, int Y, int lane, int a_end,
-                                           double bx, double by, double bz, double Rb, double twoRb, double mb,
-                                           unsigned long long rmb, bool bvalid, const TileUniform& tu,
-                                           long long h_min_bits, double Ha, double* rowA, double* rowB,
-                                           double& pe, uint32_t& rowbits, uint32_t& colbits)
-{
-    const size_t plane = (size_t)s.npad * s.npad;
-    const int B = Y * kBlock + lane;
-    for (int a = 0; a < a_end; ++a) {
-        const bool valid = bvalid && (X != Y || lane < a);
-        bool contact = false;
-        if (valid) {
-            const int A = X * kBlock + a;
-            const double Ra = ab.R[a];
-            const double sumRaRb = UNI ? tu.sum0 : Ra + Rb;              // :104
-            const double rx = bx - ab.x[a], ry = by - ab.y[a], rz = bz - ab.z[a];  // :105
-            const double d2 = rx * rx + ry * ry + rz * rz;
-            int p;
-            unsigned long long F;
-            const unsigned long long Yr = rsqrt_fix(d2, p, F);            // ~1/sqrt(d2), integer pipe
-            const double dist = sqrt_fix(d2, F, Yr, p);                   // :107, RN(sqrt)
-            const double overlap = sumRaRb - dist;                        // :110
-            // the comparisons of the step are made on the bit patterns
-            // (integer pipe): for doubles of one sign the integer order
-            // is the FP order; NaN is excluded explicitly
-            const long long ob = __double_as_longlong(overlap);
-            double fx, fy, fz;
-            if (ob > 0 && ob <= 0x7ff0000000000000ll) {                    // overlap > 0
-                contact = true;
-                const ContactIn in = gather_contact(s, A, B);
-                const ContactOut o = contact_pair_exact<WRITE>(in, s.mat, rx, ry, rz, dist, overlap, Ra, Rb,
-                                                               ab.twoR[a], twoRb, ab.fourR[a], ab.cR3[a]);
-                fx = o.fx; fy = o.fy; fz = o.fz;
-                const double im_a = s.inv_moi[A], mo_a = s.moi[A];
-                const double im_b = s.inv_moi[B], mo_b = s.moi[B];
-                double* ta = s.torqbuf + (size_t)A * s.npad + B;   // :187
-                double* tb = s.torqbuf + (size_t)B * s.npad + A;   // :188
-                ta[0] = div_by_recip(o.tax, mo_a, im_a);
-                ta[plane] = div_by_recip(o.tay, mo_a, im_a);
-                ta[2 * plane] = div_by_recip(o.taz, mo_a, im_a);
-                tb[0] = div_by_recip(o.tbx, mo_b, im_b);
-                tb[plane] = div_by_recip(o.tby, mo_b, im_b);
-                tb[2 * plane] = div_by_recip(o.tbz, mo_b, im_b);
-                if (WRITE) pe += o.pe;
-            } else {
-                long long hb = ob & 0x7fffffffffffffffll;                  // :211-215 |overlap|
-                if (hb < h_min_bits) hb = h_min_bits;                      // h < h_min (NaN stays NaN)
-                const double h = __longlong_as_double(hb);
-                const double coef = UNI ? vdw_coef_uniform(h, tu.R0, tu.twoR0, tu.c40, tu.P0)
-                                        : vdw_coef_fix(h, Ra, Rb, ab.twoR[a], twoRb, ab.fourR[a], ab.cR3[a]);
-                fx = coef * div_by_rsqrt(rx, dist, Yr, p);                    // :221-227
-                fy = coef * div_by_rsqrt(ry, dist, Yr, p);
-                fz = coef * div_by_rsqrt(rz, dist, Yr, p);
-                if (WRITE) pe += vdw_energy(Ha, h, Ra, Rb, ab.twoR[a]);                    // :239
-            }
-            // :249-250 -- acc[A] += F/m[A]; acc[B] -= F/m[B] (stored negated)
-            const double ma = ab.m[a];
-            const unsigned long long rma = ab.rm[a];
-            double* pa = rowA + (size_t)a * s.npad;
-            __stcs(pa, div_by_fixed<false>(fx, ma, rma));
-            __stcs(pa + plane, div_by_fixed<false>(fy, ma, rma));
-            __stcs(pa + 2 * plane, div_by_fixed<false>(fz, ma, rma));
-            double* pb = rowB + a;
-            __stcs(pb, div_by_fixed<false, true>(fx, mb, rmb));  // -(F/m[B]), sign set in the integer result
-            __stcs(pb + plane, div_by_fixed<false, true>(fy, mb, rmb));
-            __stcs(pb + 2 * plane, div_by_fixed<false, true>(fz, mb, rmb));
-        }
-        const uint32_t bal = __ballot_sync(0xffffffffu, contact);
-        if (lane == a) rowbits = bal;
-        if (contact) colbits |= 1u << a;
-    }
-}
-
 // One warp per lower-triangular 32x32 block tile (X, Y), X >= Y.  Lane b
 // owns sphere B = 32Y + b and walks the 32 spheres A = 32X + a of the A
 // block; on the diagonal only a > b is a pair.  Tiles are independent; one

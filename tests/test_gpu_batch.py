@@ -32,11 +32,15 @@ def _instances():
     return cols
 
 
-def test_exact_batch_matches_single_system_runs():
+@pytest.mark.parametrize("shape", [(64, 128), (0, 128)])
+def test_exact_batch_matches_single_system_runs(shape):
+    """Both exact pair passes -- the per-sphere loop and the pair-tile pass
+    (each pair once into per-CTA buffers, then ordered row sums) -- are bit
+    for bit the single-system step, hence the reference's."""
     cols = _instances()
     steps, skip = 40, 10
     run = B.BatchRun(cols, "exact", steps=steps, skip=skip)
-    run.set_shape(64, 128)
+    run.set_shape(*shape)
     run.run(1, steps, do_init=True)
     assert not run.status().any()
     st = run.state()
@@ -64,17 +68,18 @@ def test_exact_batch_matches_single_system_runs():
 def test_batch_shapes_agree_and_autotuner_picks_one():
     cols = _instances()
     results = []
-    for tile, threads in ((32, 64), (128, 256)):
+    for tile, threads in ((32, 64), (128, 256), (0, 128), (0, 256)):
         run = B.BatchRun(cols, "exact", steps=10, skip=5)
         run.set_shape(tile, threads)
         run.run(1, 10, do_init=True)
         results.append(run.state())
-    for k in STATE:
-        assert np.array_equal(results[0][k], results[1][k])
+    for r in results[1:]:  # the pair-tile pass (tile 0) too: bit for bit
+        for k in STATE:
+            assert np.array_equal(results[0][k], r[k])
     run = B.BatchRun(cols, "exact", steps=10, skip=5)
     tuned = run.autotune(sample_steps=2)
-    assert tuned["tile"] in (32, 64, 128) and tuned["threads"] in (64, 128, 256)
-    assert len(tuned["times_ms"]) == 9  # the pair-tile pass is the mixed form's
+    assert tuned["tile"] in (0, 32, 64, 128) and tuned["threads"] in (64, 128, 256)
+    assert len(tuned["times_ms"]) == 12
     assert all(t > 0 for t in tuned["times_ms"].values())
     run.run(1, 10, do_init=True)   # the autotuner restored the initial state
     st = run.state()
