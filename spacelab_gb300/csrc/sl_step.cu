@@ -85,7 +85,7 @@ __device__ __forceinline__ void col_tile_coords(int nb, long long u, int& X, int
 }
 
 template <bool WRITE>
-__global__ void __launch_bounds__(128, 3) pair_tile_kernel(const __grid_constant__ System s, int c0, int c1)
+__global__ void __launch_bounds__(128, 4) pair_tile_kernel(const __grid_constant__ System s, int c0, int c1)
 {
     __shared__ ABlock sA[4];
     const int lane = threadIdx.x & 31;
@@ -332,7 +332,7 @@ __global__ void stage_out_kernel(const __grid_constant__ System s, const __grid_
 int pair_grid_blocks(long long tiles, int num_sms)
 {
     long long want = (tiles + 3) / 4;
-    long long cap = (long long)num_sms * 3;  // 3 CTAs (12 warps) per SM
+    long long cap = (long long)num_sms * 4;  // 4 CTAs (16 warps) per SM
     return (int)(want < cap ? want : cap);
 }
 
