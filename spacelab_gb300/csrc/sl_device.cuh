@@ -68,8 +68,10 @@ struct System {
     // (c, K, i) is component c of sphere i's acceleration terms from the
     // partners in 32-sphere block K
     float* f_part;
-    // mixed form: the pair kernel's tile counter (zeroed by the drift kernel)
+    // mixed form: the pair kernel's tile counter, and per sphere a flag set
+    // when any of its pairs is in contact (both zeroed by the drift kernel)
     int* tile_counter;
+    int* contact_flag;
     int len_shift;
     // mixed form: squared separation factor of the far-pair paths
     // (far_threshold_sq in sl_pair_mixed.cuh)

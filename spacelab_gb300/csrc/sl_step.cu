@@ -46,6 +46,7 @@ __global__ void __launch_bounds__(kDriftThreads) drift_kernel(const __grid_const
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 3 * s.n) return;
     if (t == 0 && s.tile_counter) *s.tile_counter = 0;  // the mixed pair kernel's work queue
+    if (t < s.n && s.contact_flag) s.contact_flag[t] = 0;
     const int c = t / s.n;
     const int i = t - c * s.n;
     const double dt = s.sc->dt;

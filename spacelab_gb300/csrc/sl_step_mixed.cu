@@ -250,12 +250,15 @@ __global__ void __launch_bounds__(32 * kPairWarps, kPairCtasPerSm) mixed_pair_ke
             P[o + pplane] = fmaf(ima, ay, -inv_mb * bsy);
             P[o + 2 * pplane] = fmaf(ima, az, -inv_mb * bsz);
             s.cmask[o] = rowbits | colbits;
+            if (rowbits | colbits) s.contact_flag[iA] = 1;
         } else {
             const size_t oa = (size_t)Y * s.npad + iA, ob = (size_t)X * s.npad + B;
             P[oa] = ima * ax; P[oa + pplane] = ima * ay; P[oa + 2 * pplane] = ima * az;
             P[ob] = -inv_mb * bsx; P[ob + pplane] = -inv_mb * bsy; P[ob + 2 * pplane] = -inv_mb * bsz;
             s.cmask[oa] = rowbits;
             s.cmask[ob] = colbits;
+            if (rowbits) s.contact_flag[iA] = 1;  // every writer stores 1
+            if (colbits) s.contact_flag[B] = 1;
         }
         if (WRITE) {
             if (qn > 0 && t + nwarps >= s.ntiles) flush_near(qn);  // the warp's last tile
@@ -296,6 +299,8 @@ __global__ void __launch_bounds__(32 * kFinSlices) mixed_finish_kernel(const __g
     const size_t plane = (size_t)s.npad * s.npad;
     const float* p = s.f_part + i;
     const uint32_t* mk = s.cmask + i;
+    // contact words only for spheres with a contact this step (few)
+    const bool any_contact = i < s.n && s.contact_flag[i] != 0;
     const float* tb = reinterpret_cast<const float*>(s.torqbuf) + (size_t)i * s.npad;
     df::Sum f[3] = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}};
     df::Sum tq[3] = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}};
@@ -317,7 +322,7 @@ __global__ void __launch_bounds__(32 * kFinSlices) mixed_finish_kernel(const __g
             const size_t o = (size_t)(K + u) * s.npad;
 #pragma unroll
             for (int c = 0; c < 3; ++c) v[c][u] = __ldcs(p + o + c * pplane);
-            m[u] = __ldcs(mk + o);
+            m[u] = any_contact ? __ldcs(mk + o) : 0u;
         }
 #pragma unroll
         for (int u = 0; u < U; ++u) {
@@ -330,7 +335,7 @@ __global__ void __launch_bounds__(32 * kFinSlices) mixed_finish_kernel(const __g
         const size_t o = (size_t)K * s.npad;
 #pragma unroll
         for (int c = 0; c < 3; ++c) f[c].add(__ldcs(p + o + c * pplane));
-        torques(__ldcs(mk + o), K);
+        torques(any_contact ? __ldcs(mk + o) : 0u, K);
     }
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
