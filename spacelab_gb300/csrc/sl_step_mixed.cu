@@ -93,7 +93,7 @@ __global__ void __launch_bounds__(32 * kPairWarps, kPairCtasPerSm) mixed_pair_ke
     int2* q = queue_all[WRITE ? wib : 0];
     int qn = 0;
     double pe = 0;
-    auto flush_near = [&](int cnt) {  // pairs q[0 .. cnt), cnt <= 32; the rest move down
+    auto flush_close = [&](int cnt) {  // pairs q[0 .. cnt), cnt <= 32; the rest move down
         if (lane < cnt) {
             const int A = q[lane].x, B = q[lane].y;
             const double d2_64 = fp64_d2(s, A, B), sum64 = s.R[A] + s.R[B];
@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(32 * kPairWarps, kPairCtasPerSm) mixed_pair_ke
                         if (need) q[qn + __popc(m & ((1u << lane) - 1u))] = make_int2(X * kBlock + r, B);
                         qn += __popc(m);
                         __syncwarp();
-                        if (qn >= kBlock) flush_near(kBlock);
+                        if (qn >= kBlock) flush_close(kBlock);
                     }
                 }
                 if (!FULL && !valid) fx = fy = fz = 0.0f;
@@ -261,7 +261,7 @@ __global__ void __launch_bounds__(32 * kPairWarps, kPairCtasPerSm) mixed_pair_ke
             if (colbits) s.contact_flag[B] = 1;
         }
         if (WRITE) {
-            if (qn > 0 && t + nwarps >= s.ntiles) flush_near(qn);  // the warp's last tile
+            if (qn > 0 && t + nwarps >= s.ntiles) flush_close(qn);  // the warp's last tile
             pe += -s.mat.Ha / 6 * (f2d_bits(pe_far.s) + f2d_bits(pe_far.c));
             for (int off = 16; off > 0; off >>= 1) pe += __shfl_xor_sync(0xffffffffu, pe, off);
             if (lane == 0) s.pe_tile[t] = pe;
