@@ -277,7 +277,7 @@ __global__ void __launch_bounds__(32 * kPairWarps, kPairCtasPerSm) mixed_pair_ke
     }
 }
 
-constexpr int kFinSlices = 16;
+constexpr int kFinSlices = 8;
 
 // Per-sphere totals, then pass 3.  Block = 32 spheres (lanes) x kFinSlices
 // warps; warp w adds partner blocks [nb w / S, nb (w+1) / S) of its lane's
