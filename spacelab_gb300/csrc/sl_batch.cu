@@ -8,14 +8,17 @@
 // another.  Within an instance a step is the reference's three passes
 // (ColliderSingleCore.cpp:82-97, 100-256, 263-287):
 //   drift    one thread per sphere (strided);
-//   pairs    i-centric: thread i walks partners j ascending through j-tiles
-//            staged in shared memory and adds each term to its running sum
-//            in the order the reference adds them to acc[i] -- the result is
-//            bit-identical to the reference step, pair terms being computed
-//            in the reference's (A = max, B = min) orientation;
+//   pairs    either the pair-tile pass (shape tile 0: every pair once into
+//            the CTA's pair-term buffers by the single system's tile routine,
+//            then ordered row sums), or the per-sphere loop: thread i walks
+//            partners j ascending through j-tiles staged in shared memory and
+//            adds each term to its running sum in the order the reference
+//            adds them to acc[i].  Either way the result is bit-identical to
+//            the reference step, pair terms being computed in the
+//            reference's (A = max, B = min) orientation;
 //   kick     pass 3, plus the write-step energy totals reduced in a fixed
 //            tree inside the CTA.
-// The j-tile size (template) and threads per instance (block size) are
+// The pass, its j-tile size and the threads per instance (block size) are
 // chosen by the host autotuner (sl_batch_capi.cu).
 #include "sl_batch.h"
 #include "sl_batch_common.cuh"

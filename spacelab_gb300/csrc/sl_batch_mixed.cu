@@ -1,12 +1,15 @@
 // sl_batch_mixed.cu -- batched solver in the mixed-precision form: the same
-// persistent work-queue launch as sl_batch.cu, with the pair pass of the
+// persistent work-queue launch as sl_batch.cu, with the pair math of the
 // mixed form: far pairs entirely in FP32 (no square root), close pairs with
 // double-float (sl_df.cuh) displacement, |r|^2 and squared gap from the
-// double-float positions the drift writes; FP32 forces and torques; FP32
-// sums per j-tile joined in compensated per-sphere totals, converted to
-// FP64; FP64 kin/kout test and write-step potential energy of close pairs
-// from the FP64 positions (far pairs: the FP32 series of vdw_bracket).
-// The non-contact pair path issues no FP64 instruction.
+// double-float positions the drift writes; FP32 forces and torques; FP64
+// kin/kout test and write-step potential energy of close pairs from the
+// FP64 positions (far pairs: the FP32 series of vdw_bracket).  The
+// non-contact pair path issues no FP64 instruction.  Two pair passes over
+// each instance's Z-ordered slots (sl_batch.h): the pair-tile pass (shape
+// tile 0, every pair once, per-CTA partial sums) and the per-sphere loop
+// (j-tiles of 32/64/128, every pair from both sides, FP32 sums per j-tile
+// joined in compensated per-sphere totals).
 #include "sl_batch.h"
 #include "sl_batch_common.cuh"
 #include "sl_df.cuh"
