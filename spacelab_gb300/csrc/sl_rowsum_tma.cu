@@ -153,26 +153,35 @@ __global__ void __launch_bounds__(32 * kRsWarps, 8 / BPS) rowsum_tma_kernel(cons
         waited = 1;
     }
     for (int q = 0; ok && q < nq; ++q) {
+        // The add chain is the critical path: the bookkeeping of the stages
+        // sits between its first chunks, each of which leaves the warp
+        // waiting on the FP64 add latency anyway.
+        acc.add_chunk(cur[0]);
         __syncwarp();  // every lane has stage q in registers: its buffer is free
         if (lane == 0 && q + kRsStages < nq) {
             tma::fence_proxy_async();
             rs_issue<T, BPS>(buf, full, &map, q + kRsStages, x0, row0);
         }
+        acc.add_chunk(cur[1]);
+        bool have_next = false;
         if (q + 1 < nq) {
             const int st1 = (q + 1) % kRsStages;
             ok = __all_sync(0xffffffffu, tma::mbar_wait(&full[st1], ((q + 1) / kRsStages) & 1));
-            if (ok) {
+            have_next = ok;
+        }
+        acc.add_chunk(cur[2]);
+        if (have_next) {
+            const int st1 = (q + 1) % kRsStages;
 #pragma unroll
-                for (int k = 0; k < Stage::kChunks; ++k) nxt[k] = rs_chunk(buf + st1 * Stage::kBytes, lane, k);
-                waited = q + 2;
-            }
+            for (int k = 0; k < Stage::kChunks; ++k) nxt[k] = rs_chunk(buf + st1 * Stage::kBytes, lane, k);
+            waited = q + 2;
         }
 #pragma unroll
         for (int pb = 0; pb < kBps; ++pb) {  // each partner block in the stage
             constexpr int kChunksPerBlock = Stage::kChunks / kBps;
 #pragma unroll
             for (int k = pb * kChunksPerBlock; k < (pb + 1) * kChunksPerBlock; ++k) {
-                acc.add_chunk(cur[k]);
+                if (k >= 3) acc.add_chunk(cur[k]);
             }
             if (q % kSpb == kSpb - 1) {  // partner block Y complete: its torque terms
                 const int Y = b0 + (q / kSpb) * kBps + pb;
