@@ -68,12 +68,17 @@ def _metric(w, mode: str) -> str:
     return f"pair-interactions/s at N={w.n} ({'FP64' if mode == 'exact' else 'mixed FP32/FP64'} {w.name})"
 
 
-def _config(w, extra=None):
+def _config(w, extra=None, mode: str = "exact"):
     npad = (w.n + 31) // 32 * 32
+    if mode == "exact":
+        l2 = (f"per-step working set > L2: the pair-term buffer (3*npad^2 terms, "
+              f"{3 * npad * npad * 8 / 1e6:.0f} MB as FP64) is streamed through HBM every step")
+    else:  # mixed: per-tile partials and contact words, 16 B per (sphere, partner block)
+        ws = 16 * npad * (npad // 32) / 1e6
+        l2 = (f"mixed form, no pair-term buffer: per-step working set {ws:.0f} MB of tile partials and contact "
+              f"words, {'above' if ws > 129 else 'within'} the 129 MB L2; no flush between steps")
     cfg = {"workload": w.name, "n_spheres": w.n, "steps_per_write": w.skip,
-           "dt_s": w.dt, "kin": w.kin, "kout": w.kout, "seeds": w.info,
-           "l2": f"per-step working set > L2: the pair-term buffer (3*npad^2 terms, "
-                 f"{3 * npad * npad * 8 / 1e6:.0f} MB as FP64) is streamed through HBM every step"}
+           "dt_s": w.dt, "kin": w.kin, "kout": w.kout, "seeds": w.info, "l2": l2}
     if w.name == "aggregate_collision_n5000":
         cfg.update({"n_target": 4000, "n_projectile": 1000})
     if extra:
@@ -261,7 +266,7 @@ def run_ours(args, rank, world, local_rank) -> dict | None:
         "vs_baseline": None, "dtype": "f64" if args.mode == "exact" else "f32+f64",
         "data": "synthetic (seeded clusters; no dataset)",
         "config": _config(w, {"parallelism": "replicas" if world > 1 else "single GPU", "mode": args.mode,
-                               "overlap": bool(args.overlap)}),
+                               "overlap": bool(args.overlap)}, mode=args.mode),
         "impl": "ours",
         "e2e": e2e,
         "gpu_launches": gpu_launches,
