@@ -1,11 +1,12 @@
 // sl_capi.cu -- the extern "C" handle API of include/spacelab_gpu.h.
 //
 // A handle owns one device arena holding the structure-of-arrays state of
-// one system, the per-pair scratch (pairbuf/torqbuf/cmask) and the energy
-// reduction buffers, plus a CUDA stream and, for sl_run, an instantiated
-// CUDA graph of one write interval.  The caller's vec3[n] (AoS) arrays are
-// copied as they are, one copy per array, into a device staging area, and a
-// kernel transposes them to or from the SoA state.
+// one system, the per-pair scratch (pairbuf/torqbuf/cmask; the mixed form's
+// per-tile partials instead of pairbuf) and the energy reduction buffers,
+// plus a CUDA stream and, for sl_run, an instantiated CUDA graph of one write
+// interval.  A kernel transposes the caller's vec3[n] (AoS) arrays to or from
+// the SoA state, reading and writing them in place where the GPU can reach
+// them, otherwise through a device staging area and one copy per array.
 #include "../../include/spacelab_gpu.h"
 #include "sl_device.cuh"
 #include "sl_kernels.h"
