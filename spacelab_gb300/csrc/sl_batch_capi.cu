@@ -212,7 +212,9 @@ int sl_batch_create(int ninst, const int* counts, const sl_material* mat, int mo
     b.part_nb = (max_n + sl::kBlock - 1) / sl::kBlock;
     b.part_np = b.part_nb * sl::kBlock;
     b.part_cta = 6 * (size_t)b.part_nb * b.part_np;
-    b.part_ctas = h->num_sms * sl::kTileCtasPerSm;
+    // no more CTAs than instances ever run at once
+    const long long max_ctas = std::min<long long>((long long)h->num_sms * sl::kTileCtasPerSm, ninst);
+    b.part_ctas = (int)max_ctas;
     const size_t o_part = take(mode == SL_MODE_MIXED ? b.part_cta * b.part_ctas * sizeof(float) : 0);
     // exact: the pair-tile pass's per-CTA pair terms, torques and contact
     // words at the largest instance's padded size, where that fits the
@@ -228,8 +230,8 @@ int sl_batch_create(int ninst, const int* counts, const sl_material* mat, int mo
         size_t free_b = 0, total_b = 0;
         if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) free_b = 0;
         const long long fit = (long long)(std::min(kExactTileScratchBytes, free_b / 3) / per_cta);
-        const long long ctas = std::min<long long>((long long)h->num_sms * sl::kTileCtasPerSm, fit);
-        if (ctas >= h->num_sms) {
+        const long long ctas = std::min<long long>(max_ctas, fit);
+        if (ctas >= std::min<long long>(h->num_sms, ninst)) {
             exact_tiles = true;
             b.part_ctas = (int)ctas;
             o_xpair = take(b.xpair_cta * ctas * sizeof(double));
