@@ -22,6 +22,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 from pathlib import Path
 
@@ -92,14 +93,24 @@ class ClockSampler:
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
+    # SL_CLOCKS_DIR: where the raw nvidia-smi samples are kept (default: a
+    # temporary file, removed after it is summarised).
     def __init__(self, gpu_index: int):
         self.proc = None
-        self.path = ROOT / "gpurun_out" / f"clocks_rank{gpu_index}.csv"
         self.gpu = gpu_index
+        keep = os.environ.get("SL_CLOCKS_DIR")
+        if keep:
+            self.path = Path(keep) / f"clocks_rank{gpu_index}.csv"
+            self.keep = True
+        else:
+            fd, name = tempfile.mkstemp(prefix=f"sl_clocks{gpu_index}_", suffix=".csv")
+            os.close(fd)
+            self.path = Path(name)
+            self.keep = False
 
     def start(self):
         try:
-            self.path.parent.mkdir(exist_ok=True)
+            self.path.parent.mkdir(parents=True, exist_ok=True)
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
                                           "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
@@ -109,6 +120,8 @@ class ClockSampler:
 
     def stop(self) -> dict:
         if self.proc is None:
+            if not self.keep:
+                self.path.unlink(missing_ok=True)
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.proc.terminate()
         try:
@@ -118,7 +131,10 @@ class ClockSampler:
         self.fh.close()
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.path.read_text().splitlines():
+        text = self.path.read_text()
+        if not self.keep:
+            self.path.unlink(missing_ok=True)
+        for line in text.splitlines():
             parts = [p.strip() for p in line.split(",")]
             if len(parts) < 9:
                 continue
