@@ -270,6 +270,7 @@ def run_ours(args, rank, world, local_rank) -> dict | None:
 
     # end to end through the C ABI with host buffers (upload + step + download)
     e2e = run_e2e(sim, w, min(args.steps, 60))
+    pair_kernel = sim.pair_kernel()
     sim.close()
 
     if world > 1:
@@ -287,7 +288,7 @@ def run_ours(args, rank, world, local_rank) -> dict | None:
         "e2e": e2e,
         "gpu_launches": gpu_launches,
         "roofline": {"bound": "fp64" if args.mode == "exact" else "fp32",
-                     "kernel": "pair_tile_kernel" if args.mode == "exact" else "mixed_pair_kernel",
+                     "kernel": pair_kernel,
                      "achieved": achieved_tflops,
                      "peak": peak_tflops, "unit": "TFLOP/s", "frac": achieved_tflops / peak_tflops,
                      "traffic": traffic,

@@ -155,6 +155,12 @@ int sl_set_overlap(sl_handle* h, int enable);
 /* Kernel launches one step makes (a write step computes the energy too). */
 int sl_step_launches(const sl_handle* h, int write, int* count);
 
+/* Name of the pair kernel the handle's steps launch: "pair_tile_kernel"
+ * (exact mode), "mixed_pair_kernel" or, for large systems in mixed mode,
+ * "mixed_pair2_kernel" (two column blocks per work item).  The string is
+ * static. */
+int sl_pair_kernel(const sl_handle* h, const char** name);
+
 /* Per-kernel timing: when enabled, every step records CUDA events around
  * the pair kernel and the row-sum kernel; sl_kernel_times returns their
  * accumulated milliseconds and launch counts since the last reset.  With

@@ -228,6 +228,12 @@ class GpuStep:
         check(self._lib.sl_step_launches(self._h, int(write), ctypes.byref(c)), "sl_step_launches")
         return c.value
 
+    def pair_kernel(self) -> str:
+        """Name of the pair kernel this handle's steps launch."""
+        c = ctypes.c_char_p()
+        check(self._lib.sl_pair_kernel(self._h, ctypes.byref(c)), "sl_pair_kernel")
+        return c.value.decode()
+
     def kernel_timing(self, enable: bool) -> None:
         check(self._lib.sl_kernel_timing(self._h, int(enable)), "sl_kernel_timing")
 

@@ -190,6 +190,7 @@ __device__ void make_view(System& v, const Batch& b, int inst, int off, int n)
     v.nb = (n + kBlock - 1) / kBlock;
     v.npad = b.x_np;  // the scratch's row stride
     v.ntiles = (long long)v.nb * (v.nb + 1) / 2;
+    v.nitems = v.ntiles;
     const Vec3Soa* src[8] = {&b.pos, &b.prev, &b.vel, &b.velh, &b.w, &b.wh, &b.acc, &b.aacc};
     Vec3Soa* dst[8] = {&v.pos, &v.prev, &v.vel, &v.velh, &v.w, &v.wh, &v.acc, &v.aacc};
     for (int k = 0; k < 8; ++k)

@@ -229,6 +229,8 @@ int sl_create(int n, const sl_material* mat, int mode, sl_handle** out)
     s.npad = (n + sl::kBlock - 1) / sl::kBlock * sl::kBlock;
     s.nb = s.npad / sl::kBlock;
     s.ntiles = (long long)s.nb * (s.nb + 1) / 2;
+    s.pair_double = mode == SL_MODE_MIXED && sl::mixed_pair_double(s.nb, h->num_sms);
+    s.nitems = s.pair_double ? sl::mixed_pair_items(s.nb) : s.ntiles;
     s.mat = sl::Material{mat->G, mat->Ha, mat->u_s, mat->u_r, mat->h_min};
     const size_t np = s.npad;
     const size_t A = 256;
@@ -248,7 +250,7 @@ int sl_create(int n, const sl_material* mat, int mode, sl_handle** out)
     const size_t o_pair = take(mixed ? 3 * (size_t)s.nb * np * sizeof(float) : 3 * np * np * sizeof(double));
     const size_t o_torq = take(3 * np * np * (mixed ? sizeof(float) : sizeof(double)));
     const size_t o_mask = take(np * s.nb * sizeof(uint32_t));
-    const size_t o_pe = take((size_t)s.ntiles * sizeof(double));
+    const size_t o_pe = take((size_t)s.nitems * sizeof(double));
     const size_t o_red = take(sl::kRedBlocks * 8 * sizeof(double));
     const size_t o_en = take(8 * sizeof(double));
     const size_t o_st = take(sizeof(unsigned int));
@@ -575,6 +577,16 @@ int sl_step_launches(const sl_handle* h, int write, int* count)
         np = sl::phase_bounds(h->sys.nb, cb);
     }
     *count = 1 + 2 * np + (write ? 2 : 0);  // drift, pair + row-sum per phase, energy
+    return SL_OK;
+}
+
+int sl_pair_kernel(const sl_handle* h, const char** name)
+{
+    if (int r = check_handle(h)) return r;
+    if (!name) return fail(SL_ERR_ARG, "name is NULL");
+    *name = h->mode == SL_MODE_EXACT ? "pair_tile_kernel"
+            : h->sys.pair_double     ? "mixed_pair2_kernel"
+                                     : "mixed_pair_kernel";
     return SL_OK;
 }
 

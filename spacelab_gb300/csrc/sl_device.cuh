@@ -44,6 +44,9 @@ struct Vec3Soa {
 struct System {
     int n, npad, nb;
     long long ntiles;  // nb * (nb + 1) / 2 lower-triangular block tiles
+    long long nitems;  // pair-kernel work items, one pe_tile entry each: ntiles, or
+                       // mixed_pair_items(nb) where pair_double is set
+    int pair_double;   // mixed form: two column blocks per work item
     Vec3Soa pos, prev, vel, velh, w, wh, acc, aacc;
     double *R, *m, *moi, *twoR, *fourR, *cR3;
     unsigned long long* rm;  // 64-bit fixed-point reciprocal significand of m (recip_sig)
@@ -51,7 +54,7 @@ struct System {
     double* pairbuf;      // [3][npad][npad]
     double* torqbuf;      // [3][npad][npad]
     uint32_t* cmask;      // [npad][nb]
-    double* pe_tile;      // [ntiles]
+    double* pe_tile;      // [nitems]
     double* red;          // [kRedBlocks][8] energy partials
     double* energy;       // [8] PE, KE, mom xyz, L xyz
     unsigned int* status; // error bits (see SL_ERR_* in spacelab_gpu.h)
@@ -155,6 +158,18 @@ __device__ __forceinline__ double div_by_recip(double a, double b, double y)
 }
 
 // Lower-triangular tile index t -> (X, Y), X >= Y, t = X(X+1)/2 + Y.
+// Work items of the mixed pair kernel: the lower-triangular 32 x 32 block
+// tiles grouped in 64 x 64 macro tiles (P, Q), P >= Q, of block rows 2P and
+// 2P + 1 and block columns 2Q and 2Q + 1.  Item 2m + h of macro tile m is row
+// block X = 2P + h against column blocks 2Q and 2Q + 1, both below X when
+// P > Q; when P == Q, h = 0 is the diagonal tile (X, X) alone and h = 1 takes
+// the tiles (X, X - 1) and (X, X).  An item whose row block X >= nb is empty.
+__host__ __device__ inline long long mixed_pair_items(int nb)
+{
+    const long long m = (nb + 1) / 2;
+    return m * (m + 1);
+}
+
 __device__ __forceinline__ void tile_coords(long long t, int& X, int& Y)
 {
     // FP32 estimate (the FP64 pipe is slow), corrected exactly below

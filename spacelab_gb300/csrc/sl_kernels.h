@@ -50,6 +50,9 @@ void launch_rowsum_tma(const System& s, const CUtensorMap& map, int b0, int b1, 
 // Status bit set by a kernel whose bounded wait for a TMA copy ran out.
 constexpr unsigned kStatusWaitTimeoutBit = 2u;
 void launch_step_mixed(const System& s, bool write, int num_sms, cudaStream_t st, StepTimers* tm);
+// Whether the mixed pair kernel takes two column blocks per item (mixed_pair_items)
+// for nb row blocks on num_sms SMs: where each warp takes many items.
+bool mixed_pair_double(int nb, int num_sms);
 void launch_drift(const System& s, cudaStream_t st);
 void launch_energy(const System& s, cudaStream_t st);
 int pair_grid_blocks(long long tiles, int num_sms);

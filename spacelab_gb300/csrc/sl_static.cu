@@ -84,6 +84,7 @@ sl::System static_system(double* base, int n, const sl_material& mat)
     s.npad = (n + sl::kBlock - 1) / sl::kBlock * sl::kBlock;
     s.nb = s.npad / sl::kBlock;
     s.ntiles = (long long)s.nb * (s.nb + 1) / 2;
+    s.nitems = s.ntiles;
     // pairbuf/torqbuf rows are s.npad long; they fit the kNp x kNp capacity
     sl::Vec3Soa* vecs[8] = {&s.pos, &s.prev, &s.vel, &s.velh, &s.w, &s.wh, &s.acc, &s.aacc};
     for (int v = 0; v < 8; ++v)

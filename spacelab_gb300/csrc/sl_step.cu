@@ -251,7 +251,7 @@ __global__ void __launch_bounds__(kRedThreads) energy_final_kernel(const __grid_
     __shared__ double sh[8][kRedThreads];
     const int tid = threadIdx.x;
     double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    for (long long t = tid; t < s.ntiles; t += kRedThreads) v[0] += s.pe_tile[t];
+    for (long long t = tid; t < s.nitems; t += kRedThreads) v[0] += s.pe_tile[t];
     for (int b = tid; b < nred; b += kRedThreads)
         for (int k = 0; k < 7; ++k) v[k + 1] += s.red[b * 8 + k];
 #pragma unroll

@@ -30,7 +30,10 @@
 // the 32 steps lane l holds row l's sum.  The tile then writes one FP32
 // partial per sphere and component, and mixed_finish_kernel adds a sphere's
 // partials over the partner blocks in ascending order in compensated sums.
-// Every order is fixed, so runs repeat bit for bit.
+// Every order is fixed, so runs repeat bit for bit.  Large systems
+// (mixed_pair_double) take a row block against two column blocks at a time
+// (mixed_pair2_kernel): one shared-memory load of a row and one shuffle then
+// serve two pairs.
 //
 // The physics follows ColliderSingleCore.cpp:104-253 term by term; only the
 // arithmetic and the evaluation order differ.
@@ -53,6 +56,10 @@ namespace {
 constexpr int kRowStride = 12;
 constexpr int kPairWarps = 4;
 constexpr int kPairCtasPerSm = 5;  // resident CTAs per SM (the launch bounds' minimum)
+constexpr int kPair2CtasPerSm = 4;  // the same for two column blocks per item (127 registers)
+// Two column blocks per item pay where the warps take many items each;
+// with few, the longer items leave the last ones on fewer warps.
+constexpr int kDoubleMinTilesPerWarp = 8;
 
 // |pos[B] - pos[A]|^2 in FP64, the formula of the previous-step distance in
 // contact_mixed (rare paths: the contact test, write-step energies).
@@ -277,6 +284,306 @@ __global__ void __launch_bounds__(32 * kPairWarps, kPairCtasPerSm) mixed_pair_ke
     }
 }
 
+// A lane's column sphere of a tile (scaled lengths; its radius's lo part and
+// 1/m are read where they are needed, which keeps two of these in registers).
+struct ColSphere {
+    float x, y, z, xl, yl, zl;  // position, hi and lo parts
+    float R, R3;
+    int B;
+};
+
+__device__ __forceinline__ ColSphere load_col(const System& s, int B)
+{
+    ColSphere c;
+    c.B = B;
+    c.x = s.f_pos[0][B]; c.y = s.f_pos[1][B]; c.z = s.f_pos[2][B];
+    c.xl = s.f_pos[3][B]; c.yl = s.f_pos[4][B]; c.zl = s.f_pos[5][B];
+    c.R = s.f_R[B];
+    c.R3 = c.R * c.R * c.R;
+    return c;
+}
+
+// One warp per work item (mixed_pair_items): row block X against one or two
+// column blocks, rows A = 32X + r above columns B = 32Y + b.  With two, a
+// lane holds the column spheres b of both column blocks, so that one
+// shared-memory load of row r and one shuffle of its running sum serve two
+// pairs.  Writes the partials f_part[c][K][i] (sphere i's terms from partner
+// block K; a row sphere's terms from both column blocks go to the first, the
+// second gets 0, or on the diagonal the sphere's terms as a column), contact
+// bits to cmask[K][i] and torques of contacts to the float view of torqbuf,
+// [A][B] and [B][A].
+template <bool WRITE>
+__global__ void __launch_bounds__(32 * kPairWarps, kPair2CtasPerSm) mixed_pair2_kernel(const __grid_constant__ System s)
+{
+    __shared__ __align__(16) float rows_all[kPairWarps][kBlock * kRowStride];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    float* rows = rows_all[wib];
+    const long long nwarps = (long long)gridDim.x * kPairWarps;
+    const size_t plane = (size_t)s.npad * s.npad;  // torque planes
+    const size_t pplane = (size_t)s.nb * s.npad;   // partial planes
+    float* tbuf = reinterpret_cast<float*>(s.torqbuf);
+    const int sh = s.len_shift;
+    const float L = ldexpf(1.0f, sh);
+    const float hmin_s = (float)s.mat.h_min / L;
+    const float c_vdw = (float)(s.mat.Ha / 6 * 64) / L;   // dyn per unit vdw_shape
+    const int nxt = (lane + 1) & (kBlock - 1);
+    // write steps: close pairs out of contact whose FP64 potential is pending.
+    // Their FP64 evaluation runs with every lane busy (the FP64 pipe takes a
+    // warp instruction per ~64 cycles however few lanes are active)
+    __shared__ int2 queue_all[WRITE ? kPairWarps : 1][WRITE ? 2 * kBlock : 1];
+    int2* q = queue_all[WRITE ? wib : 0];
+    int qn = 0;
+    double pe = 0;
+    auto flush_close = [&](int cnt) {  // pairs q[0 .. cnt), cnt <= 32; the rest move down
+        if (lane < cnt) {
+            const int A = q[lane].x, B = q[lane].y;
+            const double d2_64 = fp64_d2(s, A, B), sum64 = s.R[A] + s.R[B];
+            pe += pair_pe_fp64(s.mat, s.R[A], s.R[B], fma(sum64, sum64, -d2_64), d2_64, false, 0.0);
+        }
+        const int left = qn - cnt;
+        const int2 e = lane < left ? q[cnt + lane] : make_int2(0, 0);
+        __syncwarp();
+        if (lane < left) q[lane] = e;
+        __syncwarp();
+        qn = left;
+    };
+    // lane l's bits are the rows in contact with its column sphere; returns
+    // the transpose: lane l's bits are the columns in contact with row l
+    auto transpose = [&](uint32_t colbits) {
+        uint32_t rowbits = 0;
+        if (__any_sync(0xffffffffu, colbits != 0u)) {
+            for (int r = 0; r < kBlock; ++r) {
+                const uint32_t wd = __ballot_sync(0xffffffffu, (colbits >> r) & 1u);
+                if (lane == r) rowbits = wd;
+            }
+        }
+        return rowbits;
+    };
+
+    // Items: a first round in warp order, then, on plain steps, whichever
+    // warp is free takes the next item from a counter that the drift kernel
+    // zeroes (the last round of a static stride leaves SMs idle); write
+    // steps keep the static stride, so that their close-pair queues, and so
+    // the potential energy's rounding, repeat run to run.
+    long long t = (long long)blockIdx.x * kPairWarps + wib;
+    for (; t < s.nitems;) {
+        int P, Q;
+        tile_coords(t >> 1, P, Q);
+        const int X = 2 * P + (int)(t & 1);
+        pe = 0;
+        df::Sum pe_far{0.0f, 0.0f};  // far pairs' vdW brackets (write steps)
+        if (X < s.nb) {
+            {
+                const int i = X * kBlock + lane;  // < npad
+                const float Ri = s.f_R[i];
+                float* row = rows + lane * kRowStride;
+                *reinterpret_cast<float4*>(row) = make_float4(s.f_pos[0][i], s.f_pos[1][i], s.f_pos[2][i], Ri);
+                *reinterpret_cast<float4*>(row + 4) =
+                    make_float4(s.f_pos[3][i], s.f_pos[4][i], s.f_pos[5][i], c_vdw * (Ri * Ri * Ri));
+                row[8] = s.f_Rlo[i];
+                row[9] = s.f_inv_m[i];
+            }
+            __syncwarp();
+            const int nA = s.n - X * kBlock;       // rows r < nA are spheres
+            const bool single = P == Q && !(t & 1);  // the diagonal tile (X, X) alone
+            const bool diag1 = P == Q;               // (two column blocks) the second is X
+            const ColSphere c0 = load_col(s, (single ? X : 2 * Q) * kBlock + lane);
+
+            // pairs out of contact with h = |r| - R_A - R_B above the clamp
+            // h_min, in FP32 (scaled lengths): the vdW force (:205-226)
+            // Ra^3 Rb^3 (h + Ra + Rb) / (S^2 T^2) along r/|r| needs no square
+            // root: h + Ra + Rb = |r|, S = h (h + 2(Ra + Rb)) = |r|^2 - (Ra + Rb)^2
+            // and T = S + 4 Ra Rb = |r|^2 - (Ra - Rb)^2; used for |r| >= 1.25
+            // (Ra + Rb) or more, where S cancels little (far_sq).  The force
+            // on the row sphere; d2 = |r|^2 and sum2 = (Ra + Rb)^2 for the test.
+            auto far_force = [&](const float4& q0, const float4& q1, const ColSphere& c, float& d2, float& sum2,
+                                 float& fx, float& fy, float& fz) {
+                const float rx = (c.x - q0.x) + (c.xl - q1.x);
+                const float ry = (c.y - q0.y) + (c.yl - q1.y);
+                const float rz = (c.z - q0.z) + (c.zl - q1.z);
+                d2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
+                const float sumR = q0.w + c.R, difR = q0.w - c.R;
+                sum2 = sumR * sumR;
+                const float S = d2 - sum2;
+                const float T = fmaf(-difR, difR, d2);
+                const float Pst = S * T;
+                const float fr = (q1.w * c.R3) * rcp_approx(Pst * Pst);  // |F| / |r|
+                fx = fr * rx; fy = fr * ry; fz = fr * rz;
+            };
+            // close pair (row r, column sphere c): double-float (~48 bits, FP32
+            // pipe) subtraction, |r|^2 and squared gap g = (R_A + R_B)^2 - |r|^2,
+            // then the contact branch or the clamped vdW; true in contact
+            auto close_pair = [&](int r, const float4& q0, const float4& q1, const ColSphere& c, uint32_t& bits,
+                                  float& fx, float& fy, float& fz) {
+                const int A = X * kBlock + r, B = c.B;
+                const float Ras = q0.w;
+                const df::F2 drx = df::sub({c.x, c.xl}, {q0.x, q1.x});
+                const df::F2 dry = df::sub({c.y, c.yl}, {q0.y, q1.y});
+                const df::F2 drz = df::sub({c.z, c.zl}, {q0.z, q1.z});
+                const df::F2 dd2 = df::add(df::add(df::sqr(drx), df::sqr(dry)), df::sqr(drz));
+                const df::F2 sum = df::add({Ras, rows[r * kRowStride + 8]}, {c.R, s.f_Rlo[B]});
+                const df::F2 gap2 = df::sub(df::sqr(sum), dd2);
+                const float d2s = dd2.hi;
+                const float inv_dn = rsqrtf(d2s);
+                const float dist_s = d2s * inv_dn;
+                const float ovl_s = __fdividef(gap2.hi, Ras + c.R + dist_s);
+                const float nx = drx.hi * inv_dn, ny = dry.hi * inv_dn, nz = drz.hi * inv_dn;
+                if (gap2.hi > 0.0f || (gap2.hi == 0.0f && gap2.lo > 0.0f)) {
+                    bits |= 1u << r;
+                    const ContactIn in = gather_contact(s, A, B);
+                    // the kin/kout test compares |r|^2 with the previous step's,
+                    // both in FP64 from the FP64 positions with one formula
+                    const double d2_64 = fp64_d2(s, A, B);
+                    const ContactF o = contact_mixed(in, s.mat, sh, d2_64, nx, ny, nz, dist_s * L, ovl_s * L, Ras,
+                                                     c.R);
+                    fx = o.fx; fy = o.fy; fz = o.fz;
+                    const float ima = s.f_inv_moi[A], imb = s.f_inv_moi[B];
+                    float* ta = tbuf + (size_t)A * s.npad + B;
+                    float* tb = tbuf + (size_t)B * s.npad + A;
+                    ta[0] = o.tax * ima; ta[plane] = o.tay * ima; ta[2 * plane] = o.taz * ima;
+                    tb[0] = o.tbx * imb; tb[plane] = o.tby * imb; tb[2 * plane] = o.tbz * imb;
+                    if (WRITE) {
+                        const double sum64 = s.R[A] + s.R[B];
+                        pe += pair_pe_fp64(s.mat, s.R[A], s.R[B], fma(sum64, sum64, -d2_64), d2_64, true, o.k);
+                    }
+                    return true;
+                }
+                const float hn = fmaxf(-ovl_s, hmin_s);                 // :211-215
+                const float f = c_vdw * vdw_shape(hn, Ras, c.R);
+                fx = f * nx; fy = f * ny; fz = f * nz;
+                return false;
+            };
+            // write steps only: the far pair's vdW bracket, or the close pair
+            // out of contact queued for its FP64 potential (32 at a time)
+            auto write_terms = [&](bool valid, bool closep, bool contact, float d2, float Ras, const ColSphere& c,
+                                   int r) {
+                if (valid && !closep) pe_far.add(vdw_bracket(d2, Ras, c.R));
+                const bool need = valid && closep && !contact;
+                const uint32_t m = __ballot_sync(0xffffffffu, need);
+                if (m) {
+                    if (need) q[qn + __popc(m & ((1u << lane) - 1u))] = make_int2(X * kBlock + r, c.B);
+                    qn += __popc(m);
+                    __syncwarp();
+                    if (qn >= kBlock) flush_close(kBlock);
+                }
+            };
+
+            uint32_t bits0 = 0, bits1 = 0;      // contact rows of the lane's column spheres
+            float ax = 0, ay = 0, az = 0;       // running sum of row (lane + k) mod 32 at step k
+            float b0x = 0, b0y = 0, b0z = 0;    // column sphere sums
+            float b1x = 0, b1y = 0, b1z = 0;
+            const int iA = X * kBlock + lane;
+            const float ima = rows[lane * kRowStride + 9];
+            float* Pt = s.f_part;
+            if (single) {
+#pragma unroll 2
+                for (int k = 0; k < kBlock; ++k) {
+                    const int r = (lane + k) & (kBlock - 1);
+                    const bool valid = r < nA && lane < r;
+                    const float4 q0 = *reinterpret_cast<const float4*>(rows + r * kRowStride);
+                    const float4 q1 = *reinterpret_cast<const float4*>(rows + r * kRowStride + 4);
+                    float d2, sum2, fx, fy, fz;
+                    far_force(q0, q1, c0, d2, sum2, fx, fy, fz);
+                    const bool closep = d2 < s.far_sq * sum2;
+                    bool contact = false;
+                    if (valid && closep) contact = close_pair(r, q0, q1, c0, bits0, fx, fy, fz);
+                    if (WRITE) write_terms(valid, closep, contact, d2, q0.w, c0, r);
+                    if (!valid) fx = fy = fz = 0.0f;
+                    ax += fx; ay += fy; az += fz;
+                    b0x += fx; b0y += fy; b0z += fz;
+                    ax = __shfl_sync(0xffffffffu, ax, nxt);
+                    ay = __shfl_sync(0xffffffffu, ay, nxt);
+                    az = __shfl_sync(0xffffffffu, az, nxt);
+                }
+                // lane l now holds row l's sum; sphere iA is both row and column
+                const uint32_t rowbits = transpose(bits0);
+                const size_t o = (size_t)X * s.npad + iA;
+                Pt[o] = fmaf(ima, ax, -ima * b0x);
+                Pt[o + pplane] = fmaf(ima, ay, -ima * b0y);
+                Pt[o + 2 * pplane] = fmaf(ima, az, -ima * b0z);
+                s.cmask[o] = rowbits | bits0;
+                if (rowbits | bits0) s.contact_flag[iA] = 1;
+            } else {
+                const ColSphere c1 = load_col(s, (2 * Q + 1) * kBlock + lane);
+                // FULL: both column blocks below X and every row a sphere (the
+                // column blocks below X are full)
+                auto sweep = [&](auto full_tag) {
+                    constexpr bool FULL = decltype(full_tag)::value;
+#pragma unroll 2
+                    for (int k = 0; k < kBlock; ++k) {
+                        const int r = (lane + k) & (kBlock - 1);
+                        const bool v0 = FULL || r < nA;
+                        const bool v1 = FULL || (r < nA && (!diag1 || lane < r));
+                        const float4 q0 = *reinterpret_cast<const float4*>(rows + r * kRowStride);
+                        const float4 q1 = *reinterpret_cast<const float4*>(rows + r * kRowStride + 4);
+                        float d20, s20, f0x, f0y, f0z, d21, s21, f1x, f1y, f1z;
+                        far_force(q0, q1, c0, d20, s20, f0x, f0y, f0z);
+                        far_force(q0, q1, c1, d21, s21, f1x, f1y, f1z);
+                        const bool cl0 = d20 < s.far_sq * s20, cl1 = d21 < s.far_sq * s21;
+                        bool ct0 = false, ct1 = false;
+                        if (v0 && cl0) ct0 = close_pair(r, q0, q1, c0, bits0, f0x, f0y, f0z);
+                        if (v1 && cl1) ct1 = close_pair(r, q0, q1, c1, bits1, f1x, f1y, f1z);
+                        if (WRITE) {
+                            write_terms(v0, cl0, ct0, d20, q0.w, c0, r);
+                            write_terms(v1, cl1, ct1, d21, q0.w, c1, r);
+                        }
+                        if (!FULL) {
+                            if (!v0) f0x = f0y = f0z = 0.0f;
+                            if (!v1) f1x = f1y = f1z = 0.0f;
+                        }
+                        ax += f0x + f1x; ay += f0y + f1y; az += f0z + f1z;
+                        b0x += f0x; b0y += f0y; b0z += f0z;
+                        b1x += f1x; b1y += f1y; b1z += f1z;
+                        ax = __shfl_sync(0xffffffffu, ax, nxt);
+                        ay = __shfl_sync(0xffffffffu, ay, nxt);
+                        az = __shfl_sync(0xffffffffu, az, nxt);
+                    }
+                };
+                if (!diag1 && (X + 1) * kBlock <= s.n)
+                    sweep(std::true_type{});
+                else
+                    sweep(std::false_type{});
+                // lane l now holds row l's sum over both column blocks
+                const uint32_t rb0 = transpose(bits0), rb1 = transpose(bits1);
+                const size_t oa0 = (size_t)(2 * Q) * s.npad + iA, oa1 = oa0 + s.npad;
+                const size_t ob0 = (size_t)X * s.npad + c0.B, ob1 = (size_t)X * s.npad + c1.B;
+                Pt[oa0] = ima * ax; Pt[oa0 + pplane] = ima * ay; Pt[oa0 + 2 * pplane] = ima * az;
+                const float imb0 = s.f_inv_m[c0.B], imb1 = s.f_inv_m[c1.B];
+                Pt[ob0] = -imb0 * b0x; Pt[ob0 + pplane] = -imb0 * b0y; Pt[ob0 + 2 * pplane] = -imb0 * b0z;
+                s.cmask[oa0] = rb0;
+                s.cmask[ob0] = bits0;
+                if (diag1) {  // column sphere c1 is the row sphere iA: its partners after it in block X
+                    Pt[oa1] = -imb1 * b1x; Pt[oa1 + pplane] = -imb1 * b1y; Pt[oa1 + 2 * pplane] = -imb1 * b1z;
+                    s.cmask[oa1] = rb1 | bits1;
+                } else {
+                    Pt[oa1] = 0.0f; Pt[oa1 + pplane] = 0.0f; Pt[oa1 + 2 * pplane] = 0.0f;
+                    Pt[ob1] = -imb1 * b1x; Pt[ob1 + pplane] = -imb1 * b1y; Pt[ob1 + 2 * pplane] = -imb1 * b1z;
+                    s.cmask[oa1] = rb1;
+                    s.cmask[ob1] = bits1;
+                }
+                if (rb0 | rb1) s.contact_flag[iA] = 1;  // every writer stores 1
+                if (bits0) s.contact_flag[c0.B] = 1;
+                if (bits1) s.contact_flag[c1.B] = 1;
+            }
+        }
+        if (WRITE) {
+            if (qn > 0 && t + nwarps >= s.nitems) flush_close(qn);  // the warp's last item
+            pe += -s.mat.Ha / 6 * (f2d_bits(pe_far.s) + f2d_bits(pe_far.c));
+            for (int off = 16; off > 0; off >>= 1) pe += __shfl_xor_sync(0xffffffffu, pe, off);
+            if (lane == 0) s.pe_tile[t] = pe;
+        }
+        __syncwarp();
+        if (WRITE) {
+            t += nwarps;
+        } else {
+            int k = 0;
+            if (lane == 0) k = atomicAdd(s.tile_counter, 1);
+            t = nwarps + __shfl_sync(0xffffffffu, k, 0);
+        }
+    }
+}
+
 constexpr int kFinSlices = 8;
 
 // Per-sphere totals, then pass 3.  Block = 32 spheres (lanes) x kFinSlices
@@ -369,17 +676,32 @@ __global__ void __launch_bounds__(32 * kFinSlices) mixed_finish_kernel(const __g
 
 }  // namespace
 
+bool mixed_pair_double(int nb, int num_sms)
+{
+    const long long ntiles = (long long)nb * (nb + 1) / 2;
+    const long long warps = (long long)num_sms * kPair2CtasPerSm * kPairWarps;
+    return ntiles >= kDoubleMinTilesPerWarp * warps;
+}
+
 void launch_step_mixed(const System& s, bool write, int num_sms, cudaStream_t st, StepTimers* tm)
 {
     launch_drift(s, st);
     if (tm) cudaEventRecord(tm->ev[0], st);
-    long long want = (s.ntiles + kPairWarps - 1) / kPairWarps;
-    long long cap = (long long)num_sms * kPairCtasPerSm;  // one wave of persistent warps
+    long long want = (s.nitems + kPairWarps - 1) / kPairWarps;
+    // one wave of persistent warps
+    long long cap = (long long)num_sms * (s.pair_double ? kPair2CtasPerSm : kPairCtasPerSm);
     const int pb = (int)(want < cap ? want : cap);
-    if (write)
-        mixed_pair_kernel<true><<<pb, 32 * kPairWarps, 0, st>>>(s);
-    else
-        mixed_pair_kernel<false><<<pb, 32 * kPairWarps, 0, st>>>(s);
+    if (s.pair_double) {
+        if (write)
+            mixed_pair2_kernel<true><<<pb, 32 * kPairWarps, 0, st>>>(s);
+        else
+            mixed_pair2_kernel<false><<<pb, 32 * kPairWarps, 0, st>>>(s);
+    } else {
+        if (write)
+            mixed_pair_kernel<true><<<pb, 32 * kPairWarps, 0, st>>>(s);
+        else
+            mixed_pair_kernel<false><<<pb, 32 * kPairWarps, 0, st>>>(s);
+    }
     if (tm) cudaEventRecord(tm->ev[1], st);
     mixed_finish_kernel<<<s.nb, 32 * kFinSlices, 0, st>>>(s);
     if (tm) cudaEventRecord(tm->ev[2], st);

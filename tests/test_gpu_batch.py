@@ -87,7 +87,7 @@ def test_batch_shapes_agree_and_autotuner_picks_one():
         assert np.array_equal(st[k], results[0][k])
 
 
-@pytest.mark.parametrize("shape", [(64, 128), (0, 256), (0, 64), (0, 512)])
+@pytest.mark.parametrize("shape", [(64, 128), (0, 256), (0, 64), (0, 128), (0, 512)])
 def test_mixed_batch_tracks_exact_batch(shape):
     """Both mixed pair passes: the per-sphere partner loop (j-tiles of 64)
     and the pair-tile pass (tile 0: each pair once, Z-ordered 32-sphere

@@ -31,10 +31,14 @@ def _sim(c, mode):
     return s
 
 
-@pytest.mark.parametrize("n,seed", [(2, 1), (65, 2), (300, 3)])
+# 7000 spheres: 24,090 block tiles, enough for the pair kernel to take two
+# column blocks per work item on a GB300 (mixed_pair_double)
+@pytest.mark.parametrize("n,seed", [(2, 1), (65, 2), (300, 3), (7000, 4)])
 def test_mixed_step0_forces_and_contacts(n, seed):
     c = contact_case(n, seed)
     ex, mx = _sim(c, "exact"), _sim(c, "mixed")
+    assert ex.pair_kernel() == "pair_tile_kernel"
+    assert mx.pair_kernel() == ("mixed_pair2_kernel" if n == 7000 else "mixed_pair_kernel")
     ee, em = ex.init_conditions(), mx.init_conditions()
     assert np.array_equal(ex.contacts(), mx.contacts())
     ge, gm = ex.download(), mx.download()
@@ -67,8 +71,9 @@ def test_mixed_trajectory_and_energy_track_fp64():
     assert np.abs(gm.pos - ge.pos).max() <= 1e-2 * c["R"].max()
 
 
-def test_mixed_looper_is_deterministic():
-    c = contact_case(256, 9)
+@pytest.mark.parametrize("n", [256, 7000])
+def test_mixed_looper_is_deterministic(n):
+    c = contact_case(n, 9)
     a, b = _sim(c, "mixed"), _sim(c, "mixed")
     a.init_conditions(); b.init_conditions()
     ra = a.sim_looper(steps=41, skip=10)
