@@ -56,7 +56,7 @@ namespace {
 constexpr int kRowStride = 12;
 constexpr int kPairWarps = 4;
 constexpr int kPairCtasPerSm = 5;  // resident CTAs per SM (the launch bounds' minimum)
-constexpr int kPair2CtasPerSm = 4;  // the same for two column blocks per item (127 registers)
+constexpr int kPair2CtasPerSm = 4;  // the same for two column blocks per item (128 registers, no spills)
 // Two column blocks per item pay where the warps take many items each;
 // with few, the longer items leave the last ones on fewer warps.
 constexpr int kDoubleMinTilesPerWarp = 8;
