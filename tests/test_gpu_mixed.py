@@ -31,14 +31,16 @@ def _sim(c, mode):
     return s
 
 
-# 7000 spheres: 24,090 block tiles, enough for the pair kernel to take two
-# column blocks per work item on a GB300 (mixed_pair_double)
-@pytest.mark.parametrize("n,seed", [(2, 1), (65, 2), (300, 3), (7000, 4)])
+# 6500 and 7000 spheres: 20,910 and 24,090 block tiles, enough for the pair
+# kernel to take two column blocks per work item on a GB300
+# (mixed_pair_double); 204 row blocks (the last of 4 spheres) and 219 (an odd
+# count, with empty items)
+@pytest.mark.parametrize("n,seed", [(2, 1), (65, 2), (300, 3), (6500, 5), (7000, 4)])
 def test_mixed_step0_forces_and_contacts(n, seed):
     c = contact_case(n, seed)
     ex, mx = _sim(c, "exact"), _sim(c, "mixed")
     assert ex.pair_kernel() == "pair_tile_kernel"
-    assert mx.pair_kernel() == ("mixed_pair2_kernel" if n == 7000 else "mixed_pair_kernel")
+    assert mx.pair_kernel() == ("mixed_pair2_kernel" if n >= 6500 else "mixed_pair_kernel")
     ee, em = ex.init_conditions(), mx.init_conditions()
     assert np.array_equal(ex.contacts(), mx.contacts())
     ge, gm = ex.download(), mx.download()
