@@ -18,7 +18,7 @@ the reference.  Bars (stated per quantity):
 import numpy as np
 import pytest
 
-from cases import contact_case, material
+from cases import contact_case, material, two_sphere_case
 from spacelab_gb300 import BallGroup, GpuStep, configs
 
 pytestmark = pytest.mark.gpu
@@ -115,5 +115,24 @@ def test_mixed_separated_lattice_forces_and_potential(spacing):
     assert len(ex.contacts()) == 0 and len(mx.contacts()) == 0
     ge, gm = ex.download(), mx.download()
     scale = np.abs(ge.acc).max()
+    assert np.abs(gm.acc - ge.acc).max() <= 1e-5 * scale
+    assert abs(em.PE - ee.PE) <= 5e-6 * abs(ee.PE)
+
+
+@pytest.mark.parametrize("gap", [0.2, 0.25 * (1 - 1e-6), 0.25, 0.25 * (1 + 1e-6), 0.3])
+def test_mixed_far_pair_threshold_is_seamless(gap):
+    """Two spheres at |r| = (1 + gap) (R_A + R_B) around the far-pair
+    threshold, 1.25 radii sums for these radii and h_min: below it the pair
+    takes the double-float close path and its potential is FP64, above it the
+    FP32 force without a square root and the FP32 series of the vdW bracket.
+    Both sides must agree with the FP64 exact form to the far-pair bars:
+    accelerations within 1e-5, PE within 5e-6 relative."""
+    c = two_sphere_case(gap)
+    ex, mx = _sim(c, "exact"), _sim(c, "mixed")
+    ee, em = ex.init_conditions(), mx.init_conditions()
+    assert len(ex.contacts()) == 0 and len(mx.contacts()) == 0
+    ge, gm = ex.download(), mx.download()
+    scale = np.abs(ge.acc).max()
+    assert scale > 0
     assert np.abs(gm.acc - ge.acc).max() <= 1e-5 * scale
     assert abs(em.PE - ee.PE) <= 5e-6 * abs(ee.PE)
