@@ -520,30 +520,35 @@ def main(argv=None) -> int:
     ap.add_argument("--nt-min", type=int, default=64)
     ap.add_argument("--nt-max", type=int, default=1600)
     args = ap.parse_args(argv)
-    if args.warmup < 3:
-        ap.error("--warmup must be >= 3")
+    # at least 3 untimed warm-up steps: a smaller request is raised, and the
+    # line's "warmup" reports the steps actually run
+    warmup_requested = args.warmup
+    args.warmup = max(args.warmup, 3)
     rank, world, local_rank = _dist_env()
+
+    def emit(res):
+        if warmup_requested != args.warmup:
+            res["warmup_requested"] = warmup_requested
+        print(json.dumps(res), flush=True)
+
     if args.impl == "reference":
         res = run_reference(args, rank, world)
         if res is not None:
-            print(json.dumps(res), flush=True)
+            emit(res)
         return 0
     if args.drift_steps:
-        res = run_drift(args)
-        print(json.dumps(res), flush=True)
+        emit(run_drift(args))
         return 0
     if args.batched:
-        res = run_batched(args)
-        print(json.dumps(res), flush=True)
+        emit(run_batched(args))
         return 0
     if args.surrogate_study:
-        res = run_surrogate_study(args)
-        print(json.dumps(res), flush=True)
+        emit(run_surrogate_study(args))
         return 0
     res = run_ours(args, rank, world, local_rank)
     if res is not None:
         res["cpu_baseline"] = cpu_oracle_rate(_workload(args.workload), budget_s=args.cpu_budget, threads=0)
-        print(json.dumps(res), flush=True)
+        emit(res)
     return 0
 
 
