@@ -129,11 +129,17 @@ class ClockSampler:
         except subprocess.TimeoutExpired:
             self.proc.kill()
         self.fh.close()
-        sm, smax, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         text = self.path.read_text()
         if not self.keep:
             self.path.unlink(missing_ok=True)
+        return self.summarize(text)
+
+    @staticmethod
+    def summarize(text: str) -> dict:
+        """Median and maximum SM clock and the throttle reasons seen in
+        nvidia-smi CSV samples of FIELDS (no header, no units)."""
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in text.splitlines():
             parts = [p.strip() for p in line.split(",")]
             if len(parts) < 9:
