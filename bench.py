@@ -72,10 +72,12 @@ def _metric(w, mode: str) -> str:
 def _config(w, extra=None, mode: str = "exact"):
     npad = (w.n + 31) // 32 * 32
     if mode == "exact":
-        l2 = (f"per-step working set > L2: the pair-term buffer (3*npad^2 terms, "
-              f"{3 * npad * npad * 8 / 1e6:.0f} MB as FP64) is streamed through HBM every step")
-    else:  # mixed: per-tile partials and contact words, 16 B per (sphere, partner block)
-        ws = 16 * npad * (npad // 32) / 1e6
+        mb = 3 * npad * npad * 8 / 1e6
+        l2 = (f"per-step working set {'above' if mb > 129 else 'within'} the 129 MB L2: the pair-term buffer "
+              f"(3*npad^2 terms, {mb:.0f} MB as FP64) is written and read every step; no flush between steps")
+    else:  # per-tile partials and contact words per (sphere, partner block):
+        # 3 FP64 + 1 word (mixed), 3 FP32 + 1 word (mixed_df)
+        ws = (28 if mode == "mixed" else 16) * npad * (npad // 32) / 1e6
         l2 = (f"mixed form, no pair-term buffer: per-step working set {ws:.0f} MB of tile partials and contact "
               f"words, {'above' if ws > 129 else 'within'} the 129 MB L2; no flush between steps")
     cfg = {"workload": w.name, "n_spheres": w.n, "steps_per_write": w.skip,
@@ -88,6 +90,95 @@ def _config(w, extra=None, mode: str = "exact"):
 
 
 # ------------------------------------------------------------------ clocks --
+class NvmlClocks:
+    """SM clock, maximum SM clock and clock-event (throttle) reasons read
+    through NVML (libnvidia-ml, by ctypes) every ~2 ms in a thread, so that
+    a timed region of a few tens of milliseconds still gets many samples.
+    Read-only: nothing is set."""
+
+    # nvmlClocksEventReason* bits
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
+               0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, device_index: int, pci: tuple[int, int, int] | None = None, period_s: float = 0.002):
+        import ctypes
+        import threading
+        self.ct = ctypes
+        self.nvml = ctypes.CDLL("libnvidia-ml.so.1")
+        if self.nvml.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        self.dev = ctypes.c_void_p()
+        rc = 1
+        if pci is not None:
+            bus = f"{pci[0]:08x}:{pci[1]:02x}:{pci[2]:02x}.0".encode()
+            rc = self.nvml.nvmlDeviceGetHandleByPciBusId_v2(ctypes.c_char_p(bus), ctypes.byref(self.dev))
+        if rc != 0:
+            rc = self.nvml.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(device_index), ctypes.byref(self.dev))
+        if rc != 0:
+            raise OSError("no NVML handle for the device")
+        self.reason_fn = getattr(self.nvml, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            self.nvml.nvmlDeviceGetCurrentClocksThrottleReasons
+        self.period = period_s
+        self.samples: list[tuple[int, int, int]] = []
+        self._stop = threading.Event()
+        self._thread = threading.Thread(target=self._loop, daemon=True)
+
+    def _read(self):
+        ct = self.ct
+        sm, smax, reasons = ct.c_uint(), ct.c_uint(), ct.c_ulonglong()
+        if self.nvml.nvmlDeviceGetClockInfo(self.dev, 1, ct.byref(sm)) != 0:  # NVML_CLOCK_SM
+            return None
+        self.nvml.nvmlDeviceGetMaxClockInfo(self.dev, 1, ct.byref(smax))
+        self.reason_fn(self.dev, ct.byref(reasons))
+        return sm.value, smax.value, reasons.value
+
+    def _loop(self):
+        while not self._stop.is_set():
+            r = self._read()
+            if r is not None:
+                self.samples.append(r)
+            time.sleep(self.period)
+
+    def start(self):
+        r = self._read()
+        if r is not None:
+            self.samples.append(r)
+        self._thread.start()
+
+    def stop(self) -> dict:
+        self._stop.set()
+        self._thread.join(timeout=2)
+        r = self._read()
+        if r is not None:
+            self.samples.append(r)
+        self.nvml.nvmlShutdown()
+        return self.summarize(self.samples)
+
+    @classmethod
+    def summarize(cls, samples) -> dict:
+        if not samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "source": "nvml"}
+        sm = [a for a, _, _ in samples]
+        reasons = sorted({name for _, _, bits in samples for bit, name in cls.REASONS.items() if bits & bit})
+        return {"sm_mhz": float(np.median(sm)), "sm_min_mhz": float(min(sm)),
+                "sm_max_mhz": float(max(b for _, b, _ in samples)), "reasons": reasons, "samples": len(samples),
+                "source": "nvml, every ~2 ms over the timed region"}
+
+
+def clock_sampler(local_rank: int):
+    """NVML sampler for the current CUDA device, else nvidia-smi."""
+    try:
+        import torch
+        p = torch.cuda.get_device_properties(local_rank)
+        pci = (int(p.pci_domain_id), int(p.pci_bus_id), int(p.pci_device_id))
+    except Exception:
+        pci = None
+    try:
+        return NvmlClocks(local_rank, pci)
+    except (OSError, AttributeError):
+        return ClockSampler(local_rank)
+
+
 class ClockSampler:
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -159,50 +250,107 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------- CPU oracle --
-def cpu_oracle_rate(w, budget_s: float, threads: int = 0) -> dict:
-    """Row-parallel CPU oracle on `threads` host threads (0 = all); steps of
-    the same workload until budget_s elapses (at least 2)."""
+def port_state_at(w, step: int, threads: int = 0):
+    """The workload's state after `step` steps of its schedule (write steps
+    every w.skip), computed by the row-parallel CPU oracle -- bit-identical
+    to the reference's own step.  Returns the oracle object (its state is
+    the end of that step)."""
     from oracle.oracle import CpuOracle
     g = w.group
     o = CpuOracle(g.pos, g.vel, g.w, g.R, g.m, g.moi, w.material, w.dt, w.kin, w.kout)
     o.init()
-    o.step(False, threads=threads)  # warm-up
+    for s in range(1, step + 1):
+        o.step(s % w.skip == 0, threads=threads)
+    return o
+
+
+def _timed_steps(step_fn, first: int, skip: int, steps: int | None, budget_s: float | None) -> tuple[int, float]:
+    """Run step_fn(write) for the schedule's steps first, first+1, ...:
+    exactly `steps` of them, or (steps None) until budget_s has passed and
+    at least 2 ran.  Returns (steps run, seconds)."""
     t0 = time.perf_counter()
-    steps = 0
+    k = 0
     while True:
-        o.step(False, threads=threads)
-        steps += 1
+        step_fn((first + k) % skip == 0)
+        k += 1
         el = time.perf_counter() - t0
-        if steps >= 2 and el >= budget_s:
-            break
+        if (steps is not None and k >= steps) or (steps is None and k >= 2 and el >= budget_s):
+            return k, el
+
+
+def cpu_oracle_rate(w, budget_s: float | None, threads: int = 0, start=None, first: int = 1,
+                    steps: int | None = None, warmup: int = 1) -> dict:
+    """Row-parallel CPU oracle (the C restatement) on `threads` host threads
+    (0 = all): `warmup` untimed steps, then `steps` timed steps or, with
+    steps None, steps until budget_s has passed.  start: an oracle whose
+    state to continue from (else the workload's initial state)."""
+    from oracle.oracle import CpuOracle
+    g = w.group
+    o = start
+    if o is None:
+        o = CpuOracle(g.pos, g.vel, g.w, g.R, g.m, g.moi, w.material, w.dt, w.kin, w.kout)
+        o.init()
+    for k in range(warmup):
+        o.step((first + k) % w.skip == 0, threads=threads)
+    n, el = _timed_steps(lambda wr: o.step(wr, threads=threads), first + warmup, w.skip, steps, budget_s)
     cores = CpuOracle.max_threads() if threads == 0 else threads
-    return {"value": w.pairs_per_step * steps / el, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{steps} steps of the N=5000 workload ({el:.1f} s), row-parallel C restatement of "
-                      f"sim_one_step (bit-identical to the reference build), {cores} threads, "
+    return {"value": w.pairs_per_step * n / el, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{n} steps from step {first + warmup} of the N={w.n} workload ({el:.2f} s), row-parallel C "
+                      f"restatement of sim_one_step (bit-identical to the reference build; restatement, not "
+                      f"reference), {cores} threads, {os.uname().machine} host"}
+
+
+def ref_pin_rate(w, budget_s: float | None, native: bool = False, start_state=None, first: int = 1,
+                 steps: int | None = None, warmup: int = 1) -> dict:
+    """The reference's own sim_one_step (oracle/_ref, compiled from the
+    reference's sources), one thread -- the reference's step is
+    single-threaded: `warmup` untimed steps, then `steps` timed steps or,
+    with steps None, steps until budget_s has passed.  start_state:
+    (pos, vel, w, acc, aacc) at the end of step first-1 (else the
+    workload's initial state)."""
+    from oracle.oracle import RefPin
+    g = w.group
+    ref = RefPin(g.pos, g.vel, g.w, g.R, g.m, g.moi, w.dt, w.kin, w.kout, native=native)
+    if start_state is not None:
+        ref.resume(*start_state)
+    for k in range(warmup):
+        ref.step((first + k) % w.skip == 0)
+    n, el = _timed_steps(ref.step, first + warmup, w.skip, steps, budget_s)
+    flags = "-O3 -march=native, contraction allowed" if native else "-O2 -ffp-contract=off"
+    return {"value": w.pairs_per_step * n / el, "unit": UNIT, "cores": 1, "kind": "reference",
+            "sample": f"{n} steps from step {first + warmup} of the N={w.n} workload ({el:.2f} s), the "
+                      f"reference's sim_one_step compiled from its sources ({flags}), 1 thread, "
                       f"{os.uname().machine} host"}
 
 
-def ref_pin_rate(w, budget_s: float) -> dict:
-    """The reference's own sim_one_step (oracle/_ref, built from the reference
-    sources where they are present), one thread, bounded sample."""
-    from oracle.oracle import RefPin
-    g = w.group
-    ref = RefPin(g.pos, g.vel, g.w, g.R, g.m, g.moi, w.dt, w.kin, w.kout)
-    ref.step(False)
-    t0 = time.perf_counter()
-    steps = 0
-    while True:
-        ref.step(False)
-        steps += 1
-        el = time.perf_counter() - t0
-        if steps >= 2 and el >= budget_s:
-            break
-    return {"value": w.pairs_per_step * steps / el, "unit": UNIT, "cores": 1, "kind": "reference",
-            "sample": f"{steps} steps of the N=5000 workload ({el:.1f} s), the reference's sim_one_step "
-                      f"compiled from its sources (-O2 -ffp-contract=off), 1 thread"}
+def cpu_baselines(w, budget_s: float) -> tuple[dict, list[dict]]:
+    """Rank 0's cpu_baseline (the reference's own step on 1 thread where it
+    was built, else the port on all cores) and the secondary lines, each on
+    a bounded sample from the workload's initial state (the CPU's cost per
+    step does not depend on how many pairs touch: contacts are O(N) of the
+    N(N-1)/2 pairs)."""
+    from oracle.oracle import ref_available
+    lines = []
+    if ref_available():
+        primary = ref_pin_rate(w, budget_s)
+        if ref_available(native=True):
+            lines.append(ref_pin_rate(w, budget_s / 2, native=True))
+        lines.append(cpu_oracle_rate(w, budget_s / 2, threads=0))
+    else:
+        primary = cpu_oracle_rate(w, budget_s, threads=0)
+    return primary, lines
 
 
 # ------------------------------------------------------------------ ours --
+def default_start_step(w) -> int:
+    """First step of the measured window minus one.  The aggregate collision
+    is measured after its clusters have met (they touch after ~1500 of its
+    5000 steps), so that contact pairs, the spring switch and friction are
+    in the timed steps; the other workloads from their start."""
+    return 2500 if w.name == "aggregate_collision_n5000" else 0
+
+
+
 def run_ours(args, rank, world, local_rank) -> dict | None:
     import torch
     torch.cuda.set_device(local_rank)
@@ -227,12 +375,19 @@ def run_ours(args, rank, world, local_rank) -> dict | None:
             torch.distributed.barrier()
             torch.cuda.synchronize()
 
-    # warm-up (writes included so both pair-kernel variants are loaded)
-    sim.sim_looper(steps=1 + args.warmup, skip=w.skip)
-    first = 1 + args.warmup
+    # advance to the start of the measured window on the GPU (untimed; the
+    # schedule's write steps included), then warm up (the kernels of both
+    # step kinds are loaded by the write steps of the advance or by the
+    # first sl_run)
+    start = default_start_step(w) if args.start_step is None else args.start_step
+    if start > 0:
+        sim.sim_looper(steps=start + 1, skip=w.skip)
+    contacts_start = int(len(sim.contacts()))
+    sim.sim_looper(steps=start + 1 + args.warmup, skip=w.skip, first_step=start + 1)
+    first = start + 1 + args.warmup
     nwrites = sum(1 for s in range(first, first + args.steps) if s % w.skip == 0)
 
-    clocks = ClockSampler(local_rank)
+    clocks = clock_sampler(local_rank)
     barrier()
     clocks.start()
     ev0 = torch.cuda.Event(enable_timing=True)
@@ -243,9 +398,11 @@ def run_ours(args, rank, world, local_rank) -> dict | None:
     barrier()
     clk = clocks.stop()
     ms = ev0.elapsed_time(ev1)
+    contacts_end = int(len(sim.contacts()))
     value, ms_max = replica_throughput(w.pairs_per_step * args.steps, ms, world, device="cuda")
     gpu_launches = sim.step_launches(False) * (args.steps - nwrites) + sim.step_launches(True) * nwrites
     pair_launches = (sim.step_launches(False) - 1) // 2
+    next_step = first + args.steps
 
     # per-step timing of the pair pass (non-write steps), same stream: with
     # the pipelined exact step the pair span holds all pair phases and the
@@ -253,6 +410,7 @@ def run_ours(args, rank, world, local_rank) -> dict | None:
     sim.kernel_timing(True)
     nk = max(10, min(50, args.steps))
     sim.step(nk, write_last=False)
+    next_step += nk
     pair_ms, rowsum_ms, launches = sim.kernel_times(reset=True)
     sim.kernel_timing(False)
     contacts = int(len(sim.contacts()))
@@ -260,22 +418,49 @@ def run_ours(args, rank, world, local_rank) -> dict | None:
     flops_launch = F.pair_flops(w.pairs_per_step, contacts, write=False)
     import ctypes
     lib = _lib.lib()
+    nsm = torch.cuda.get_device_properties(local_rank).multi_processor_count
+    sm_max = (clk.get("sm_max_mhz") or 2070.0) * 1e6
     pk = ctypes.c_double()
-    # the exact form's pair kernel runs on the FP64 pipe, the mixed form's on FP32
-    peak_fn = "sl_diag_fp64_peak" if args.mode == "exact" else "sl_diag_fp32_peak"
-    _lib.check(getattr(lib, peak_fn)(ctypes.byref(pk)), peak_fn)
-    peak_tflops = pk.value / 1e3
+    if args.mode in ("exact", "mixed"):
+        # both run on the FP64 pipe: the exact form's pair arithmetic, and
+        # the mixed form's 9 FP64 adds per pair (r, and the two spheres'
+        # FP64 sums), one FP64 lane-op each
+        peak_fn = "sl_diag_fp64_peak"
+        _lib.check(lib.sl_diag_fp64_peak(ctypes.byref(pk)), peak_fn)
+        if args.mode == "exact":
+            work, unit = flops_launch, "TFLOP/s"
+            peak = pk.value / 1e3
+            peak_source = "measured live: FP64 FMA chains (sl_diag_fp64_peak), 2 flops per FMA"
+            nominal = nsm * 2 * 2 * sm_max / 1e12
+            nominal_source = f"{nsm} SMs x 2 FP64 FMA/clock x 2 flops x {sm_max / 1e6:.0f} MHz"
+            bound = "fp64"
+        else:
+            work, unit = F.MIXED64_FP64_OPS_PER_PAIR * w.pairs_per_step, "T FP64 lane-ops/s"
+            peak = pk.value / 2 / 1e3
+            peak_source = "measured live: FP64 FMA chains (sl_diag_fp64_peak), one lane-op per FMA"
+            nominal = nsm * 2 * sm_max / 1e12
+            nominal_source = f"{nsm} SMs x 2 FP64 lane-ops/clock x {sm_max / 1e6:.0f} MHz"
+            bound = "fp64 (adds)"
+    else:
+        peak_fn = "sl_diag_fp32_peak"
+        _lib.check(lib.sl_diag_fp32_peak(ctypes.byref(pk)), peak_fn)
+        work, unit = flops_launch, "TFLOP/s"
+        peak = pk.value / 1e3
+        peak_source = "measured live: FP32 FMA chains (sl_diag_fp32_peak), 2 flops per FMA"
+        nominal = nsm * 128 * 2 * sm_max / 1e12
+        nominal_source = f"{nsm} SMs x 128 FP32 FMA/clock x 2 flops x {sm_max / 1e6:.0f} MHz"
+        bound = "fp32"
     # latency of a dependent FP64 add chain (bounds the row sums)
     chain = {}
     for wps in (1, 4):
         cy = ctypes.c_double()
         _lib.check(lib.sl_diag_fp64_add_latency(wps, 32, ctypes.byref(cy)), "sl_diag_fp64_add_latency")
         chain[f"{wps}_warps_per_sm"] = cy.value
-    achieved_tflops = flops_launch / (pair_ms_avg * 1e-3) / 1e12
+    achieved = work / (pair_ms_avg * 1e-3) / 1e12
     traffic = _read_profile_traffic() if (args.mode == "exact" and w.name == "aggregate_collision_n5000") else None
 
     # end to end through the C ABI with host buffers (upload + step + download)
-    e2e = run_e2e(sim, w, min(args.steps, 60))
+    e2e = run_e2e(sim, w, min(args.steps, 60), first_step=next_step)
     pair_kernel = sim.pair_kernel()
     sim.close()
 
@@ -289,17 +474,21 @@ def run_ours(args, rank, world, local_rank) -> dict | None:
         "vs_baseline": None, "dtype": "f64" if args.mode == "exact" else "f32+f64",
         "data": "synthetic (seeded clusters; no dataset)",
         "config": _config(w, {"parallelism": "replicas" if world > 1 else "single GPU", "mode": args.mode,
-                               "overlap": bool(args.overlap)}, mode=args.mode),
+                               "overlap": bool(args.overlap), "start_step": start,
+                               "timed_steps": [first, first + args.steps - 1], "write_steps_timed": nwrites,
+                               "contacts_at_start_step": contacts_start,
+                               "contacts_after_timed_steps": contacts_end}, mode=args.mode),
         "impl": "ours",
         "e2e": e2e,
         "gpu_launches": gpu_launches,
-        "roofline": {"bound": "fp64" if args.mode == "exact" else "fp32",
+        "roofline": {"bound": bound,
                      "kernel": pair_kernel,
-                     "achieved": achieved_tflops,
-                     "peak": peak_tflops, "unit": "TFLOP/s", "frac": achieved_tflops / peak_tflops,
+                     "achieved": achieved,
+                     "peak": peak, "unit": unit, "frac": achieved / peak,
                      "traffic": traffic,
-                     "peak_source": f"measured live: {'FP64' if args.mode == 'exact' else 'FP32'} FMA chains "
-                                    f"({peak_fn}), 2 flops per FMA",
+                     "peak_source": peak_source,
+                     "peak_nominal": nominal, "frac_of_nominal": achieved / nominal,
+                     "peak_nominal_source": nominal_source,
                      "flops_per_step": flops_launch, "pair_ms_per_step": pair_ms_avg,
                      "rowsum_exposed_ms_per_step": rowsum_ms / launches,
                      "fp64_add_chain_cycles": chain,
@@ -323,7 +512,7 @@ def _read_profile_traffic():
     return None
 
 
-def run_e2e(sim, w, steps: int) -> dict:
+def run_e2e(sim, w, steps: int, first_step: int = 1) -> dict:
     """Host-authoritative use of the drop-in: each step uploads the state from
     pinned host buffers, runs sim_one_step on the GPU and downloads it."""
     import ctypes
@@ -348,26 +537,28 @@ def run_e2e(sim, w, steps: int) -> dict:
     for k in range(steps):
         _lib.check(lib.sl_upload_resume(h, pp, pv, pw, pa, paa, ppr), "sl_upload_resume")
         prev[:] = pos
-        _lib.check(lib.sl_step(h, 1, int((k + 1) % w.skip == 0), pe), "sl_step")
+        _lib.check(lib.sl_step(h, 1, int((first_step + k) % w.skip == 0), pe), "sl_step")
         _lib.check(lib.sl_download(h, pp, pv, pw, pa, paa), "sl_download")
     el = time.perf_counter() - t0
     return {"value": w.pairs_per_step * steps / el, "unit": UNIT, "h2d_bytes_per_step": 6 * 3 * n * 8,
-            "d2h_bytes_per_step": 5 * 3 * n * 8, "steps": steps,
+            "d2h_bytes_per_step": 5 * 3 * n * 8, "steps": steps, "first_step": first_step,
             "api": "sl_upload_resume + sl_step(1) + sl_download per step"}
 
 
 # --------------------------------------------------- mixed vs FP64 report --
 def run_drift(args) -> dict:
-    """Mixed-precision form against the FP64 form on the same seed: energy
-    drift |E(t) - E(0)| / |E(0)| of each, their difference, the final
-    position and velocity error, and both throughputs."""
+    """Both mixed-precision forms against the FP64 form on the same seed:
+    energy drift |E(t) - E(0)| / |E(0)| of each run, each mixed run's
+    energy difference from the FP64 run at every write step, the final
+    position and velocity error, and every run's throughput (wall clock of
+    the whole schedule, write steps and host syncs included)."""
     import torch
     from spacelab_gb300 import GpuStep
     w = _workload(args.workload)
     out = {"metric": f"mixed vs FP64 on {w.name}", "workload": w.name, "n_spheres": w.n, "steps": args.drift_steps,
            "steps_per_write": w.skip}
     runs = {}
-    for mode in ("exact", "mixed"):
+    for mode in ("exact", "mixed", "mixed_df"):
         sim = GpuStep(w.group.copy(), w.material, mode)
         sim.set_scalars(w.dt, w.kin, w.kout)
         e0 = sim.init_conditions()
@@ -377,20 +568,26 @@ def run_drift(args) -> dict:
         el = time.perf_counter() - t0
         g = sim.download()
         runs[mode] = {"E0": e0.PE + e0.KE, "E": np.array([r.E for r in rows]), "pos": g.pos.copy(),
-                      "vel": g.vel.copy(), "pairs_per_s": w.pairs_per_step * args.drift_steps / el}
+                      "vel": g.vel.copy(), "pairs_per_s": w.pairs_per_step * args.drift_steps / el,
+                      "kernel": sim.pair_kernel()}
         sim.close()
-    ex, mx = runs["exact"], runs["mixed"]
+    ex = runs["exact"]
     E0 = abs(ex["E0"])
-    out.update({
-        "energy_drift_fp64": float(np.abs(ex["E"] - ex["E0"]).max() / E0),
-        "energy_drift_mixed": float(np.abs(mx["E"] - mx["E0"]).max() / E0),
-        "energy_mixed_minus_fp64": float(np.abs(mx["E"] - ex["E"]).max() / E0),
-        "pos_err_rel_to_size": float(np.abs(mx["pos"] - ex["pos"]).max() / np.abs(ex["pos"]).max()),
-        "pos_err_rel_to_radius": float(np.abs(mx["pos"] - ex["pos"]).max() / float(w.group.R.max())),
-        "vel_err_rel_to_max": float(np.abs(mx["vel"] - ex["vel"]).max() / np.abs(ex["vel"]).max()),
-        "pairs_per_s_fp64": ex["pairs_per_s"], "pairs_per_s_mixed": mx["pairs_per_s"],
-        "speedup_mixed_over_fp64": mx["pairs_per_s"] / ex["pairs_per_s"],
-    })
+    out["energy_drift_fp64"] = float(np.abs(ex["E"] - ex["E0"]).max() / E0)
+    out["pairs_per_s_fp64"] = ex["pairs_per_s"]
+    for mode in ("mixed", "mixed_df"):
+        mx = runs[mode]
+        out[mode] = {
+            "pair_kernel": mx["kernel"],
+            "energy_drift": float(np.abs(mx["E"] - mx["E0"]).max() / E0),
+            "energy_minus_fp64": float(np.abs(mx["E"] - ex["E"]).max() / E0),
+            "pos_err_rel_to_size": float(np.abs(mx["pos"] - ex["pos"]).max() / np.abs(ex["pos"]).max()),
+            "pos_err_rel_to_radius": float(np.abs(mx["pos"] - ex["pos"]).max() / float(w.group.R.max())),
+            "vel_err_rel_to_max": float(np.abs(mx["vel"] - ex["vel"]).max() / np.abs(ex["vel"]).max()),
+            "pairs_per_s": mx["pairs_per_s"],
+            "speedup_over_fp64": mx["pairs_per_s"] / ex["pairs_per_s"],
+        }
+    out["mixed_df_over_mixed"] = runs["mixed_df"]["pairs_per_s"] / runs["mixed"]["pairs_per_s"]
     return out
 
 
@@ -454,7 +651,7 @@ def run_surrogate_study(args) -> dict:
     train = B.sample_collisions(args.train_collisions, seed=21, nt_range=W.NT_RANGE, clearance=W.CLEARANCE,
                                 k_speed_div=W.K_SPEED_DIV)
     build_s = time.perf_counter() - t0
-    y, sim_info = W.simulate(train, steps, mode="mixed")
+    y, sim_info = W.simulate(train, steps, mode="mixed_df")
     x = W.features(train)
     ens = S.Ensemble(8, 4, members=5, seed=3)
     fit = ens.fit(x, y, epochs=args.epochs, batch=256, lr=1e-3)
@@ -474,23 +671,45 @@ def run_surrogate_study(args) -> dict:
 
 # ------------------------------------------------------------- reference --
 def run_reference(args, rank, world) -> dict | None:
+    """The reference arm: the reference's own sim_one_step (oracle/_ref,
+    compiled from its sources; single-threaded, as the reference is) over
+    the same steps of the same workload as the GPU arm -- W warm-up steps,
+    then exactly K timed steps from the same start step.  The state at the
+    start step is made by the row-parallel oracle (bit-identical to the
+    reference's step), untimed.  Secondary lines: the reference at -O3
+    -march=native, and the oracle restatement on all host cores."""
     if rank != 0:
         return None
     from oracle.oracle import ref_available
     w = _workload(args.workload)
     t0 = time.perf_counter()
+    start = default_start_step(w) if args.start_step is None else args.start_step
+    o = port_state_at(w, start) if start > 0 else None
+    state = None
+    if o is not None:
+        st = o.state()
+        state = tuple(st[k] for k in ("pos", "vel", "w", "acc", "aacc"))
+    timing = dict(first=start + 1, steps=args.steps, warmup=args.warmup)
+    secondary = []
     if ref_available():
-        # the reference's own sim_one_step (single-threaded by construction)
-        r = ref_pin_rate(w, budget_s=30.0)
+        r = ref_pin_rate(w, None, start_state=state, **timing)
+        if ref_available(native=True):
+            secondary.append(ref_pin_rate(w, None, native=True, start_state=state, **timing))
+        secondary.append(cpu_oracle_rate(w, None, threads=0, start=o, **timing))
     else:
-        r = cpu_oracle_rate(w, budget_s=30.0, threads=0)
+        r = cpu_oracle_rate(w, None, threads=0, start=o, **timing)
     ms_per_step = w.pairs_per_step / r["value"] * 1e3
+    first = start + 1 + args.warmup
+    cfg = _config(w, {"parallelism": "host threads", "start_step": start,
+                      "timed_steps": [first, first + args.steps - 1],
+                      "write_steps_timed": sum(1 for s in range(first, first + args.steps) if s % w.skip == 0)})
     return {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": 0, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded clusters; no dataset)",
-            "config": _config(w, {"parallelism": "host threads"}), "impl": "reference",
+            "config": cfg, "impl": "reference",
             "cpu_baseline": {"value": r["value"], "unit": UNIT, "cores": r["cores"], "kind": r["kind"],
                              "sample": r["sample"]},
+            "cpu_baselines_secondary": secondary,
             "e2e": {"value": r["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "wall_s": time.perf_counter() - t0}
 
@@ -501,8 +720,14 @@ def main(argv=None) -> int:
     ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU oracle timing (rank 0)")
-    ap.add_argument("--mode", choices=["exact", "mixed"], default="exact")
+    ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU baseline timing (rank 0)")
+    ap.add_argument("--start-step", type=int, default=None,
+                    help="steps of the schedule run before warm-up and the timed steps (default: 2500 for the "
+                         "aggregate collision, after its clusters have met; 0 otherwise)")
+    ap.add_argument("--mode", choices=["exact", "mixed", "mixed_df"], default="exact",
+                    help="exact: FP64, bit-identical to the reference; mixed: FP32 force arithmetic with FP64 "
+                         "displacements, overlaps and accumulation; mixed_df: the double-float variant "
+                         "(--batched runs exact or mixed_df)")
     ap.add_argument("--overlap", action="store_true",
                     help="exact mode: run the row sums beside the pair phases (sl_set_overlap)")
     ap.add_argument("--workload", choices=WORKLOADS, default="aggregate_collision_n5000")
@@ -553,7 +778,8 @@ def main(argv=None) -> int:
         return 0
     res = run_ours(args, rank, world, local_rank)
     if res is not None:
-        res["cpu_baseline"] = cpu_oracle_rate(_workload(args.workload), budget_s=args.cpu_budget, threads=0)
+        res["cpu_baseline"], res["cpu_baselines_secondary"] = cpu_baselines(_workload(args.workload),
+                                                                           budget_s=args.cpu_budget)
         emit(res)
     return 0
 

@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define SL_API_VERSION 1
+#define SL_API_VERSION 2
 
 /* status codes */
 #define SL_OK 0
@@ -49,9 +49,18 @@ extern "C" {
 
 /* arithmetic modes of the pair step */
 #define SL_MODE_EXACT 0     /* FP64, reference operation order, bit-exact */
-#define SL_MODE_MIXED 1     /* FP32 pair forces/torques on FP64 displacements and
-                               squared gaps; FP64 positions, accumulation, energy
-                               sums; deterministic, not bit-exact */
+#define SL_MODE_MIXED 1     /* FP32 force and torque arithmetic on relative
+                               displacements; FP64 positions, pair subtraction
+                               r_i - r_j, overlaps of close pairs, per-sphere
+                               force/torque accumulation and energy sums;
+                               deterministic, not bit-exact */
+#define SL_MODE_MIXED_DF 2  /* no FP64 pipe work for pairs out of contact:
+                               double-float (FP32 hi + lo, ~48 bits) pair
+                               subtraction and overlap of close pairs, FP32
+                               per-tile partial sums added in compensated
+                               double-float; FP64 positions, integration,
+                               contact k choice and energy totals;
+                               deterministic, not bit-exact */
 
 /* Material constants that the reference compiles in (dust_const.hpp:21-38):
  * G, Hamaker constant Ha, sliding and rolling friction u_s and u_r, and the
@@ -83,7 +92,14 @@ const char* sl_last_error(void);
 
 /* Allocate a system of n spheres on the current CUDA device.
  * Replaces Ball_group::allocate_group (ball_group.hpp:736-756) plus the
- * compiled-in constants of dust_const.hpp:21-38. */
+ * compiled-in constants of dust_const.hpp:21-38.
+ * 1 <= n <= 46340: beyond that the reference's own pair index
+ * A(A-1)/2+B of its `distances` array overflows an int (ball_group.hpp:741),
+ * so the reference cannot run such a system to compare with.  The GPU keeps
+ * no such array; the limit is kept so that every system accepted here is
+ * one the reference can run.  Device memory grows as 48 npad^2 bytes in
+ * SL_MODE_EXACT (pair and torque terms; 103 GB at the limit), and a failed
+ * allocation returns SL_ERR_ALLOC. */
 int sl_create(int n, const sl_material* mat, int mode, sl_handle** out);
 
 /* Free everything the handle owns.  Replaces Ball_group::freeMemory
@@ -148,17 +164,17 @@ void* sl_stream(sl_handle* h);
  * compute.  The sums keep their order, so results are bit-identical either
  * way.  Both kernels are limited by the FP64 pipe, so the overlap pays only
  * where the row sums are latency-bound and the phases stay large (about
- * +0.7% at N=20000, -5% at N=5000 on GB300).  Default: disabled.  Mixed
- * mode has no pipelined form (SL_ERR_UNSUPPORTED for enable != 0). */
+ * +0.7% at N=20000, -5% at N=5000 on GB300).  Default: disabled.  The
+ * mixed modes have no pipelined form (SL_ERR_UNSUPPORTED for enable != 0). */
 int sl_set_overlap(sl_handle* h, int enable);
 
 /* Kernel launches one step makes (a write step computes the energy too). */
 int sl_step_launches(const sl_handle* h, int write, int* count);
 
 /* Name of the pair kernel the handle's steps launch: "pair_tile_kernel"
- * (exact mode), "mixed_pair_kernel" or, for large systems in mixed mode,
- * "mixed_pair2_kernel" (two column blocks per work item).  The string is
- * static. */
+ * (exact mode), "mixed64_pair_kernel" (SL_MODE_MIXED), "mixed_pair_kernel"
+ * or, for large systems, "mixed_pair2_kernel" (two column blocks per work
+ * item; SL_MODE_MIXED_DF).  The string is static. */
 int sl_pair_kernel(const sl_handle* h, const char** name);
 
 /* Per-kernel timing: when enabled, every step records CUDA events around
@@ -193,13 +209,17 @@ int sl_device_bytes(const sl_handle* h, uint64_t* bytes);
  * returns after the work on it has finished.  Initially touching pairs take
  * k = kout, as in sl_init_forces.
  *
- * Limit: 1 <= n <= SL_STATIC_MAX_SPHERES; larger n returns SL_ERR_ARG.
+ * Limit: 1 <= n <= SL_STATIC_MAX_SPHERES; larger n returns SL_ERR_ARG, and
+ * so does a sphere whose R, m or moi is not finite and > 0.
  * Working memory is one static device array of about 3.2 MB that every GPU
  * loading this library holds until the process exits.  The first call on a
  * device looks up that array's device address (cudaGetSymbolAddress), so make
- * the first call on each device before any stream capture.  All calls share
- * the array: calls whose work overlaps on the GPU (other host threads, or
- * other streams) race and must be serialised by the caller. */
+ * the first call on each device before any stream capture.  The address is
+ * looked up again when the current context is another one than the one it
+ * came from (after cudaDeviceReset, or under a driver-API context of the
+ * caller's own), so calls after a reset work.  All calls share the array:
+ * calls whose work overlaps on the GPU (other host threads, or other
+ * streams) race and must be serialised by the caller. */
 int sl_forces_static(int n, const double* pos, const double* vel, const double* w, const double* R,
                      const double* m, const double* moi, const sl_material* mat, double kin, double kout,
                      double* acc, double* aacc, double* energy, void* stream);

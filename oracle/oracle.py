@@ -3,8 +3,10 @@
   CpuOracle  -- oracle/liboracle.so, the C restatement of the reference step
                 (sl_oracle.c), built everywhere by spacelab_gb300.build.
   RefPin     -- oracle/_ref/libslref.so, the reference's own sim_one_step
-                compiled from the reference sources (ref_harness.cpp); only
-                where the reference tree was present at build time.
+                compiled from the reference sources (ref_harness.cpp,
+                -O2 -ffp-contract=off), or oracle/_ref/libslref_native.so,
+                the same TU at -O3 -march=native (timing only); only where
+                the reference tree or its snapshot was at hand at build time.
 
 Only the tests, __graft_entry__.smoke() and bench.py's CPU-baseline legs use
 this module, as the checker; the GPU library never does.
@@ -19,6 +21,8 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 ORACLE_LIB = HERE / "liboracle.so"
 REF_LIB = HERE / "_ref" / "libslref.so"
+REF_LIB_NATIVE = HERE / "_ref" / "libslref_native.so"
+REF_LIB_GPU = HERE / "_ref" / "libslref_gpu.so"  # the reference TU with the GPU adapter (make adapter)
 _P = ctypes.POINTER(ctypes.c_double)
 
 
@@ -131,37 +135,62 @@ class CpuOracle:
         return int(_oracle_lib().slo_max_threads())
 
 
-_rlib = None
+_rlibs: dict = {}
 
 
-def ref_available() -> bool:
-    return REF_LIB.exists()
+def ref_available(native: bool = False) -> bool:
+    return (REF_LIB_NATIVE if native else REF_LIB).exists()
+
+
+def _ref_lib(native: bool, path: Path | None = None):
+    path = path or (REF_LIB_NATIVE if native else REF_LIB)
+    if path not in _rlibs:
+        # RTLD_LOCAL (ctypes' default): each build keeps its own globals
+        lib = ctypes.CDLL(str(path))
+        lib.slref_material.argtypes = [_P]
+        lib.slref_material.restype = None
+        lib.slref_init.argtypes = [ctypes.c_int, _P, _P, _P, _P, _P, _P, ctypes.c_double, ctypes.c_double,
+                                   ctypes.c_double, _P]
+        lib.slref_init.restype = ctypes.c_int
+        lib.slref_step.argtypes = [ctypes.c_int, _P]
+        lib.slref_step.restype = None
+        lib.slref_get.argtypes = [_P] * 5
+        lib.slref_get.restype = None
+        lib.slref_resume.argtypes = [_P] * 6
+        lib.slref_resume.restype = ctypes.c_int
+        lib.slref_looper.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, _P]
+        lib.slref_looper.restype = ctypes.c_char_p
+        _rlibs[path] = lib
+    return _rlibs[path]
 
 
 class RefPin:
-    """The reference's own sim_one_step (one global system per process)."""
+    """The reference's own sim_one_step (one global system per process and
+    build).  native=True selects the -O3 -march=native build, whose results
+    may differ in the last bits (contracted multiply-adds)."""
 
-    def __init__(self, pos, vel, w, R, m, moi, dt, kin, kout):
-        global _rlib
-        if _rlib is None:
-            lib = ctypes.CDLL(str(REF_LIB))
-            lib.slref_material.argtypes = [_P]
-            lib.slref_material.restype = None
-            lib.slref_init.argtypes = [ctypes.c_int, _P, _P, _P, _P, _P, _P, ctypes.c_double, ctypes.c_double,
-                                       ctypes.c_double, _P]
-            lib.slref_init.restype = ctypes.c_int
-            lib.slref_step.argtypes = [ctypes.c_int, _P]
-            lib.slref_step.restype = None
-            lib.slref_get.argtypes = [_P] * 5
-            lib.slref_get.restype = None
-            _rlib = lib
-        self.lib = _rlib
+    def __init__(self, pos, vel, w, R, m, moi, dt, kin, kout, native: bool = False, lib_path: Path | None = None):
+        self.lib = _ref_lib(native, lib_path)
         self.n = len(R)
         arrs = [np.ascontiguousarray(np.asarray(x, dtype=np.float64).reshape(-1)) for x in (pos, vel, w, R, m, moi)]
         self.e0 = np.zeros(8)
         rc = self.lib.slref_init(self.n, *[_p(a) for a in arrs], dt, kin, kout, _p(self.e0))
         if rc != 0:
             raise RuntimeError("slref_init failed")
+
+    def resume(self, pos, vel, w, acc, aacc, pos_prev=None):
+        """Continue from a saved state: acc/aacc of its last force pass and
+        the positions of the step before it (NULL = pos)."""
+        arrs = [np.ascontiguousarray(np.asarray(x, dtype=np.float64).reshape(-1)) for x in (pos, vel, w, acc, aacc)]
+        prev = None if pos_prev is None else np.ascontiguousarray(np.asarray(pos_prev, dtype=np.float64).reshape(-1))
+        if self.lib.slref_resume(*[_p(a) for a in arrs], _p(prev)) != 0:
+            raise RuntimeError("slref_resume failed")
+
+    def looper(self, prefix: str, steps: int, skip: int) -> str:
+        """The reference's sim_init_write + sim_looper into files named
+        <prefix>simData.csv, <prefix>energy.csv, <prefix>constants.csv;
+        returns the prefix the writer used."""
+        return self.lib.slref_looper(prefix.encode(), int(steps), int(skip), _p(self.e0)).decode()
 
     @staticmethod
     def material() -> tuple:

@@ -94,9 +94,16 @@ static std::string slref_dummy_dir()
 std::string path = slref_dummy_dir();
 std::string targetName = "slref_dummy_";
 
+// The reference TU.  SLREF_COLLIDER_TU names another copy of it: the
+// drop-in check (oracle/Makefile, target `adapter`) compiles the copy a
+// maintainer would have after adding the GPU adapter
+// (include/spacelab_sim_one_step_gpu.hpp) and defines SLREF_GPU_ADAPTER.
+#ifndef SLREF_COLLIDER_TU
+#define SLREF_COLLIDER_TU "ColliderSingleCore/ColliderSingleCore.cpp"
+#endif
 #define private public
 #define main reference_main
-#include "ColliderSingleCore/ColliderSingleCore.cpp"
+#include SLREF_COLLIDER_TU
 #undef main
 #undef private
 
@@ -147,6 +154,70 @@ int slref_init(int n, const double* pos, const double* vel, const double* w, con
     dt = dt_;
     slref_take_energy(energy);
     return 0;
+}
+
+// Resume a state inside the reference's global Ball_group after
+// slref_init: pos/vel/w/acc/aacc as given, and `distances` from the
+// positions of the previous step (ball_group.hpp:741; the reference stores
+// exactly those pair distances at the end of each pass 2).  NULL pos_prev =
+// pos.
+int slref_resume(const double* pos, const double* vel, const double* w, const double* acc, const double* aacc,
+                 const double* pos_prev)
+{
+    const int n = O.num_particles;
+    if (n < 1) return 1;
+    const double* prev = pos_prev ? pos_prev : pos;
+    for (int i = 0; i < n; i++) {
+        O.pos[i] = vec3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+        O.vel[i] = vec3(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2]);
+        O.w[i] = vec3(w[3 * i], w[3 * i + 1], w[3 * i + 2]);
+        O.acc[i] = vec3(acc[3 * i], acc[3 * i + 1], acc[3 * i + 2]);
+        O.aacc[i] = vec3(aacc[3 * i], aacc[3 * i + 1], aacc[3 * i + 2]);
+    }
+    for (int A = 1; A < n; A++) {
+        const vec3 pa(prev[3 * A], prev[3 * A + 1], prev[3 * A + 2]);
+        for (int B = 0; B < A; B++) {
+            const vec3 pb(prev[3 * B], prev[3 * B + 1], prev[3 * B + 2]);
+            O.distances[static_cast<long>(A) * (A - 1) / 2 + B] = (pb - pa).norm();
+        }
+    }
+    O.KE = 0; O.PE = 0; O.mom = {0, 0, 0}; O.ang_mom = {0, 0, 0};
+    return 0;
+}
+
+// The reference's own run: Ball_group::sim_init_write(prefix) (simData,
+// constants and energy files with the state and totals of the initial force
+// pass, ball_group.hpp:421-516), then sim_looper (ColliderSingleCore.cpp:
+// 291-375) for steps 1..steps_-1 with a write step every skip_ steps, which
+// appends the simData and energy rows.  Call after slref_init; init_energy
+// are its totals.  With SLREF_GPU_ADAPTER the looper's steps run on the GPU
+// through the adapter.  Returns the output prefix actually used (the writer
+// prepends a counter when files of that name exist).
+const char* slref_looper(const char* prefix, int steps_, int skip_, const double* init_energy)
+{
+    static std::string used;
+    energyBuffer.precision(12);  // as the reference's main does (:42)
+    ballBuffer.str("");
+    energyBuffer.str("");
+    O.PE = init_energy[0];
+    O.KE = init_energy[1];
+    O.mom = vec3(init_energy[2], init_energy[3], init_energy[4]);
+    O.ang_mom = vec3(init_energy[5], init_energy[6], init_energy[7]);
+    O.sim_init_write(prefix);
+    O.KE = 0; O.PE = 0; O.mom = {0, 0, 0}; O.ang_mom = {0, 0, 0};
+    simTimeElapsed = 0;
+    steps = steps_;
+    skip = skip_;
+#ifdef SLREF_GPU_ADAPTER
+    sl_gpu_begin();
+#endif
+    sim_looper();
+#ifdef SLREF_GPU_ADAPTER
+    sl_gpu_sync_host();
+    sl_gpu_end();
+#endif
+    used = output_prefix;
+    return used.c_str();
 }
 
 // One reference step; energy (8 doubles) is filled on write steps.

@@ -24,6 +24,8 @@ SL_ERR_TIMEOUT = 7
 
 SL_MODE_EXACT = 0
 SL_MODE_MIXED = 1
+API_VERSION = 2  # SL_API_VERSION of include/spacelab_gpu.h
+SL_MODE_MIXED_DF = 2
 
 _c_double_p = ctypes.POINTER(ctypes.c_double)
 _c_int_p = ctypes.POINTER(ctypes.c_int)
@@ -154,8 +156,8 @@ def load(path: Path | str = LIB_PATH) -> ctypes.CDLL:
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
-    if lib.sl_version() != 1:
-        raise ImportError(f"{path}: ABI version {lib.sl_version()} != 1")
+    if lib.sl_version() != API_VERSION:
+        raise ImportError(f"{path}: ABI version {lib.sl_version()} != {API_VERSION}")
     return lib
 
 

@@ -24,7 +24,9 @@ import numpy as np
 from . import _lib
 from ._lib import Energy, Material, SpaceLabError, check, dptr
 
-MODES = {"exact": _lib.SL_MODE_EXACT, "mixed": _lib.SL_MODE_MIXED}
+# "mixed": FP32 force/torque arithmetic with FP64 displacements, close-pair
+# overlaps and accumulation; "mixed_df": the double-float variant
+MODES = {"exact": _lib.SL_MODE_EXACT, "mixed": _lib.SL_MODE_MIXED, "mixed_df": _lib.SL_MODE_MIXED_DF}
 
 
 class BallGroup:

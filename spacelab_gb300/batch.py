@@ -144,7 +144,7 @@ class BatchRun:
               "sl_batch_autotune")
         grid = {(f"tile{tl}" if tl else "pairtiles") + f"_threads{thr}": float(times[3 * i + j])
                 for i, tl in enumerate((32, 64, 128, 0))
-                for j, thr in enumerate((128, 256, 512) if tl == 0 and self.mode == "mixed" else (64, 128, 256))
+                for j, thr in enumerate((128, 256, 512) if tl == 0 and self.mode == "mixed_df" else (64, 128, 256))
                 if times[3 * i + j] >= 0}
         return {"tile": t.value, "threads": th.value, "times_ms": grid}
 

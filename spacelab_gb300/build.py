@@ -1,6 +1,7 @@
 """Build the native parts in-tree: the CUDA step library for sm_103a, the
-C oracle (test infrastructure) and, where the reference tree is present,
-the reference's own step as the oracle's pin (oracle/_ref).
+C oracle (test infrastructure) and the reference's own step as the oracle's
+pin (oracle/_ref), from the reference tree where it is present or from the
+snapshot of its files that oracle/Makefile keeps in oracle/_ref/src.
 
     python -m spacelab_gb300.build            # everything
     python -m spacelab_gb300.build --lib      # only libspacelab_gb300.so
@@ -24,7 +25,12 @@ BUILD = ROOT / "_build"
 LIB = PKG / "libspacelab_gb300.so"
 ORACLE_DIR = ROOT / "oracle"
 ORACLE_LIB = ORACLE_DIR / "liboracle.so"
-REF_ROOT = Path("/root/reference")
+# Root of the reference tree: SPACELAB_REF_ROOT, else oracle/Makefile's
+# default (REF).  Where neither holds the reference, the snapshot in
+# oracle/_ref/src (made by an earlier build) is compiled instead.
+REF_ENV = "SPACELAB_REF_ROOT"
+REF_SNAPSHOT = ORACLE_DIR / "_ref" / "src"
+REF_LIBS = (ORACLE_DIR / "_ref" / "libslref.so", ORACLE_DIR / "_ref" / "libslref_native.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
@@ -97,13 +103,19 @@ def build_oracle(force: bool = False) -> Path:
 
 
 def build_reference_pin(force: bool = False) -> Path | None:
-    """oracle/_ref/libslref.so from the reference sources, where present."""
-    if not (REF_ROOT / "ColliderSingleCore" / "ColliderSingleCore.cpp").exists():
+    """oracle/_ref/libslref.so (and the -O3 native timing build) from the
+    reference's own sources; None where neither the reference tree nor a
+    snapshot of it is at hand."""
+    make = ["make", "-s", "-C", str(ORACLE_DIR)]
+    if os.environ.get(REF_ENV):
+        make.append(f"REF={os.environ[REF_ENV]}")
+    # refresh the snapshot where the tree is present; where it is not, make
+    # fails here and an existing snapshot is used as it is
+    subprocess.run(make + ["snapshot"], stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+    if not (REF_SNAPSHOT / "ColliderSingleCore" / "ColliderSingleCore.cpp").exists():
         return None
-    out = ORACLE_DIR / "_ref" / "libslref.so"
-    if force or _stale(out, [ORACLE_DIR / "ref_harness.cpp", ORACLE_DIR / "Makefile"]):
-        _run(["make", "-s", "-C", str(ORACLE_DIR), f"REF={REF_ROOT}", "-B" if force else "all"])
-    return out
+    _run(make + (["-B"] if force else []) + ["all"])
+    return REF_LIBS[0]
 
 
 def build_all(force: bool = False) -> None:

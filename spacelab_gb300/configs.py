@@ -99,17 +99,25 @@ def dust_cluster_1000(seed: int = 1000) -> Workload:
                     info={"seed": seed, "k_speed_cm_s": 1.0})
 
 
-def aggregate_collision_5000(seed_t: int = 4000, seed_p: int = 1001) -> Workload:
+def aggregate_collision_5000(seed_t: int = 4000, seed_p: int = 1001, k_speed: float = 2.0) -> Workload:
     """4000-sphere target + 1000-sphere projectile, 1.1 (Rt+Rp) apart along x,
     impact parameter 0.3 (Rt+Rp) along y, 100 cm/s relative speed, 5000
-    steps, energy every 100.  k from the reference formula at 10 cm/s: a
-    100 cm/s impact then overlaps ~1% of a radius, and the clusters touch
-    after ~1500 of the 5000 steps."""
+    steps, energy every 100.
+
+    k from the reference formula kConsts r_max v^2 at v = k_speed.  The
+    workload fixes the geometry, the speed and the step count, and asks the
+    contact time to span 50 steps, which leaves k to choose; it must be soft
+    enough that the clusters meet inside the 5000 steps (the projectile
+    travels ~6 radii before the first contact) and stiff enough that the
+    100 cm/s impact stays below the reference's design overlap of 10% of a
+    radius (maxOverlap, dust_const.hpp:31).  At 2 cm/s the impact overlaps
+    ~6.5% of a radius and dt = 4.1e-9 s, so the projectile covers ~20 radii
+    in the 5000 steps."""
     g = build_collision(4000, 1000, 100.0, 1.1, 0.3, seed_t, seed_p)
-    kin, kout, dt = spring_and_dt(float(g.R.max()), float(g.m.min()), 10.0)
+    kin, kout, dt = spring_and_dt(float(g.R.max()), float(g.m.min()), k_speed)
     return Workload("aggregate_collision_n5000", g, dt, kin, kout, steps=5000, skip=100,
                     info={"seed_target": seed_t, "seed_projectile": seed_p, "speed_cm_s": 100.0,
-                          "k_speed_cm_s": 10.0})
+                          "k_speed_cm_s": k_speed})
 
 
 def polydisperse_cluster_20000(seed: int = 20000) -> Workload:

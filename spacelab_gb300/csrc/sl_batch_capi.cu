@@ -55,7 +55,7 @@ namespace {
 
 int blocks_for(const sl_batch* h, int tile, int threads)
 {
-    int per_sm = sl::batch_max_blocks_per_sm(tile, threads, h->mode == SL_MODE_MIXED);
+    int per_sm = sl::batch_max_blocks_per_sm(tile, threads, h->mode == SL_MODE_MIXED_DF);
     if (per_sm < 1) per_sm = 1;
     long long blocks = (long long)per_sm * h->num_sms;
     if (tile == 0 && blocks > h->b.part_ctas) blocks = h->b.part_ctas;  // one scratch region per CTA
@@ -71,7 +71,7 @@ int launch_run(sl_batch* h, int tile, int threads, int first_step, int nsteps, i
     cudaGraph_t g;
     SLB_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     cudaMemsetAsync(h->b.counter, 0, sizeof(int), h->stream);
-    if (h->mode == SL_MODE_MIXED)
+    if (h->mode == SL_MODE_MIXED_DF)
         sl::launch_batch_mixed(h->b, tile, threads, blocks, first_step, nsteps, skip, do_init, h->stream);
     else
         sl::launch_batch_exact(h->b, tile, threads, blocks, first_step, nsteps, skip, do_init, h->stream);
@@ -163,7 +163,8 @@ int sl_batch_create(int ninst, const int* counts, const sl_material* mat, int mo
     if (!out) return sl_record_error(SL_ERR_ARG, "out is NULL");
     *out = nullptr;
     if (ninst < 1 || !counts || !mat) return sl_record_error(SL_ERR_ARG, "need ninst >= 1, counts and material");
-    if (mode != SL_MODE_EXACT && mode != SL_MODE_MIXED) return sl_record_error(SL_ERR_UNSUPPORTED, "unknown mode");
+    if (mode != SL_MODE_EXACT && mode != SL_MODE_MIXED_DF)
+        return sl_record_error(SL_ERR_UNSUPPORTED, "the batched solver runs SL_MODE_EXACT or SL_MODE_MIXED_DF");
     if (steps < 0 || skip < 1) return sl_record_error(SL_ERR_ARG, "need steps >= 0 and skip >= 1");
     if (!(mat->h_min > 0)) return sl_record_error(SL_ERR_ARG, "h_min must be > 0");
     long long total = 0;
@@ -199,14 +200,14 @@ int sl_batch_create(int ninst, const int* counts, const sl_material* mat, int mo
     for (auto& v : o_vec)
         for (auto& c : v) c = take(T * sizeof(double));
     for (auto& s : o_sc) s = take(T * sizeof(double));
-    for (auto& f : o_f) f = take(mode == SL_MODE_MIXED ? T * sizeof(float) : 0);
+    for (auto& f : o_f) f = take(mode == SL_MODE_MIXED_DF ? T * sizeof(float) : 0);
     const size_t o_order = take(ninst * sizeof(int)), o_off = take(ninst * sizeof(int)),
                  o_cnt = take(ninst * sizeof(int)), o_counter = take(sizeof(int));
     const size_t o_par = take(4 * (size_t)ninst * sizeof(double));
     const size_t o_en = take((size_t)ninst * b.nrec * 8 * sizeof(double));
     const size_t o_st = take(ninst * sizeof(unsigned));
     const size_t o_snap = take(15 * T * sizeof(double));
-    const size_t o_perm = take(mode == SL_MODE_MIXED ? T * sizeof(int) : 0);
+    const size_t o_perm = take(mode == SL_MODE_MIXED_DF ? T * sizeof(int) : 0);
     // mixed: the pair-tile pass's per-CTA partials, sized for the largest instance
     const int max_n = *std::max_element(counts, counts + ninst);
     b.part_nb = (max_n + sl::kBlock - 1) / sl::kBlock;
@@ -215,7 +216,7 @@ int sl_batch_create(int ninst, const int* counts, const sl_material* mat, int mo
     // no more CTAs than instances ever run at once
     const long long max_ctas = std::min<long long>((long long)h->num_sms * sl::kTileCtasPerSm, ninst);
     b.part_ctas = (int)max_ctas;
-    const size_t o_part = take(mode == SL_MODE_MIXED ? b.part_cta * b.part_ctas * sizeof(float) : 0);
+    const size_t o_part = take(mode == SL_MODE_MIXED_DF ? b.part_cta * b.part_ctas * sizeof(float) : 0);
     // exact: the pair-tile pass's per-CTA pair terms, torques and contact
     // words at the largest instance's padded size, where that fits the
     // budget for at least one CTA per SM
@@ -253,7 +254,7 @@ int sl_batch_create(int ninst, const int* counts, const sl_material* mat, int mo
     double** scal[8] = {&b.R, &b.m, &b.moi, &b.twoR, &b.fourR, &b.cR3, &inv_m_slot, &b.inv_moi};
     for (int k = 0; k < 8; ++k) *scal[k] = reinterpret_cast<double*>(base + o_sc[k]);
     b.rm = reinterpret_cast<unsigned long long*>(inv_m_slot);
-    if (mode == SL_MODE_MIXED) {
+    if (mode == SL_MODE_MIXED_DF) {
         b.f_R = reinterpret_cast<float*>(base + o_f[0]);
         b.f_inv_m = reinterpret_cast<float*>(base + o_f[1]);
         b.f_inv_moi = reinterpret_cast<float*>(base + o_f[2]);
@@ -369,7 +370,7 @@ int sl_batch_upload(sl_batch* h, const double* pos, const double* vel, const dou
 int sl_batch_set_shape(sl_batch* h, int tile, int threads)
 {
     if (!h) return sl_record_error(SL_ERR_ARG, "null batch");
-    const bool mixed = h->mode == SL_MODE_MIXED;
+    const bool mixed = h->mode == SL_MODE_MIXED_DF;
     const bool threads_ok = threads == 64 || threads == 128 || threads == 256 || (tile == 0 && mixed && threads == 512);
     if ((tile != 32 && tile != 64 && tile != 128 && tile != 0) || !threads_ok)
         return sl_record_error(SL_ERR_ARG,
@@ -393,7 +394,7 @@ int sl_batch_autotune(sl_batch* h, int sample_steps, int* tile, int* threads, do
     int bt = h->tile, bth = h->threads, k = 0;
     for (int ti = 0; ti < 4; ++ti)
         for (int hi = 0; hi < 3; ++hi, ++k) {
-            const bool mixed = h->mode == SL_MODE_MIXED;
+            const bool mixed = h->mode == SL_MODE_MIXED_DF;
             if (kTiles[ti] == 0 && !mixed && !h->b.xpair) {
                 if (times_ms) times_ms[k] = -1.0;
                 continue;

@@ -100,6 +100,8 @@ int check_handle(const sl_handle* h)
 void launch_mode_step(sl_handle* h, bool write, sl::StepTimers* tm)
 {
     if (h->mode == SL_MODE_MIXED)
+        sl::launch_step_mixed64(h->sys, write, h->num_sms, h->stream, tm);
+    else if (h->mode == SL_MODE_MIXED_DF)
         sl::launch_step_mixed(h->sys, write, h->num_sms, h->stream, tm);
     else
         sl::launch_step(h->sys, write, h->num_sms, h->stream, tm, h->overlap ? &h->ov : nullptr,
@@ -200,7 +202,8 @@ int sl_create(int n, const sl_material* mat, int mode, sl_handle** out)
     if (n < 1) return fail(SL_ERR_ARG, "n must be >= 1");
     if (n > 46340) return fail(SL_ERR_ARG, "n > 46340 exceeds the reference's pair index range");
     if (!mat) return fail(SL_ERR_ARG, "material is NULL");
-    if (mode != SL_MODE_EXACT && mode != SL_MODE_MIXED) return fail(SL_ERR_UNSUPPORTED, "unknown mode");
+    if (mode != SL_MODE_EXACT && mode != SL_MODE_MIXED && mode != SL_MODE_MIXED_DF)
+        return fail(SL_ERR_UNSUPPORTED, "unknown mode");
     if (!(mat->h_min > 0)) return fail(SL_ERR_ARG, "h_min must be > 0");
 
     sl_handle* h = new (std::nothrow) sl_handle();
@@ -229,7 +232,7 @@ int sl_create(int n, const sl_material* mat, int mode, sl_handle** out)
     s.npad = (n + sl::kBlock - 1) / sl::kBlock * sl::kBlock;
     s.nb = s.npad / sl::kBlock;
     s.ntiles = (long long)s.nb * (s.nb + 1) / 2;
-    s.pair_double = mode == SL_MODE_MIXED && sl::mixed_pair_double(s.nb, h->num_sms);
+    s.pair_double = mode == SL_MODE_MIXED_DF && sl::mixed_pair_double(s.nb, h->num_sms);
     s.nitems = s.pair_double ? sl::mixed_pair_items(s.nb) : s.ntiles;
     s.mat = sl::Material{mat->G, mat->Ha, mat->u_s, mat->u_r, mat->h_min};
     const size_t np = s.npad;
@@ -241,14 +244,18 @@ int sl_create(int n, const sl_material* mat, int mode, sl_handle** out)
         for (int c = 0; c < 3; ++c) o_vec[v][c] = take(np * sizeof(double));
     size_t o_sc[8];
     for (int k = 0; k < 8; ++k) o_sc[k] = take(np * sizeof(double));
+    // FP32 per-sphere constants (both mixed forms) and the double-float
+    // positions (SL_MODE_MIXED_DF only)
+    const bool mixed = mode != SL_MODE_EXACT;
+    const bool mixed_df = mode == SL_MODE_MIXED_DF;
     size_t o_f[10] = {};
-    if (mode == SL_MODE_MIXED)
-        for (int k = 0; k < 10; ++k) o_f[k] = take(np * sizeof(float));
-    // the mixed form keeps per-tile partial sums instead of pair terms, and
-    // FP32 torque terms
-    const bool mixed = mode == SL_MODE_MIXED;
-    const size_t o_pair = take(mixed ? 3 * (size_t)s.nb * np * sizeof(float) : 3 * np * np * sizeof(double));
-    const size_t o_torq = take(3 * np * np * (mixed ? sizeof(float) : sizeof(double)));
+    for (int k = 0; k < 10; ++k) o_f[k] = take(mixed && (k < 4 || mixed_df) ? np * sizeof(float) : 0);
+    // the mixed forms keep per-tile partial sums instead of pair terms (FP64
+    // in SL_MODE_MIXED, FP32 in SL_MODE_MIXED_DF), and torque terms in the
+    // same type
+    const size_t part_elem = mixed_df ? sizeof(float) : sizeof(double);
+    const size_t o_pair = take(mixed ? 3 * (size_t)s.nb * np * part_elem : 3 * np * np * sizeof(double));
+    const size_t o_torq = take(3 * np * np * (mixed_df ? sizeof(float) : sizeof(double)));
     const size_t o_mask = take(np * s.nb * sizeof(uint32_t));
     const size_t o_pe = take((size_t)s.nitems * sizeof(double));
     const size_t o_red = take(sl::kRedBlocks * 8 * sizeof(double));
@@ -269,15 +276,18 @@ int sl_create(int n, const sl_material* mat, int mode, sl_handle** out)
     double** scal[8] = {&s.R, &s.m, &s.moi, &s.twoR, &s.fourR, &s.cR3, &inv_m_slot, &s.inv_moi};
     for (int k = 0; k < 8; ++k) *scal[k] = reinterpret_cast<double*>(base + o_sc[k]);
     s.rm = reinterpret_cast<unsigned long long*>(inv_m_slot);
-    if (mode == SL_MODE_MIXED) {
+    if (mixed) {
         s.f_R = reinterpret_cast<float*>(base + o_f[0]);
         s.f_inv_m = reinterpret_cast<float*>(base + o_f[1]);
         s.f_inv_moi = reinterpret_cast<float*>(base + o_f[2]);
         s.f_Rlo = reinterpret_cast<float*>(base + o_f[3]);
-        for (int k = 0; k < 6; ++k) s.f_pos[k] = reinterpret_cast<float*>(base + o_f[4 + k]);
     }
-    if (mixed)
+    if (mixed_df)
+        for (int k = 0; k < 6; ++k) s.f_pos[k] = reinterpret_cast<float*>(base + o_f[4 + k]);
+    if (mixed_df)
         s.f_part = reinterpret_cast<float*>(base + o_pair);
+    else if (mixed)
+        s.part64 = reinterpret_cast<double*>(base + o_pair);
     else
         s.pairbuf = reinterpret_cast<double*>(base + o_pair);
     s.torqbuf = reinterpret_cast<double*>(base + o_torq);
@@ -540,7 +550,7 @@ int sl_contacts(sl_handle* h, int* pairs, long max_pairs, long* count)
     for (int A = 0; A < s.n; ++A) {
         for (int Y = 0; Y <= A / sl::kBlock; ++Y) {
             // [npad][nb] in the exact form, [nb][npad] in the mixed form
-            uint32_t wd = h->mode == SL_MODE_MIXED ? mask[(size_t)Y * s.npad + A] : mask[(size_t)A * s.nb + Y];
+            uint32_t wd = h->mode != SL_MODE_EXACT ? mask[(size_t)Y * s.npad + A] : mask[(size_t)A * s.nb + Y];
             while (wd) {
                 const int b = __builtin_ctz(wd);
                 wd &= wd - 1;
@@ -585,8 +595,9 @@ int sl_pair_kernel(const sl_handle* h, const char** name)
     if (int r = check_handle(h)) return r;
     if (!name) return fail(SL_ERR_ARG, "name is NULL");
     *name = h->mode == SL_MODE_EXACT ? "pair_tile_kernel"
-            : h->sys.pair_double     ? "mixed_pair2_kernel"
-                                     : "mixed_pair_kernel";
+            : h->mode == SL_MODE_MIXED ? "mixed64_pair_kernel"
+            : h->sys.pair_double       ? "mixed_pair2_kernel"
+                                       : "mixed_pair_kernel";
     return SL_OK;
 }
 

@@ -17,8 +17,10 @@
 //   cmask[npad][nb]                          contact bit per (s, 32-block);
 //                                            the mixed form stores it
 //                                            [nb][npad] (block-major)
-//   f_part[3][nb][npad]                      mixed form only: per-tile
-//                                            partial sums (pairbuf unused)
+//   f_part[3][nb][npad]                      double-float mixed form: per-tile
+//                                            FP32 partial sums (pairbuf unused)
+//   part64[3][nb][npad]                      FP64-accumulating mixed form:
+//                                            per-tile FP64 force partials
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -67,10 +69,14 @@ struct System {
     // of the scaled positions (x, y, z hi, then x, y, z lo), the latter
     // written by the drift kernel every step
     float *f_Rlo, *f_pos[6];
-    // the mixed form's per-tile partial sums [3][nb][npad] (FP32): entry
-    // (c, K, i) is component c of sphere i's acceleration terms from the
-    // partners in 32-sphere block K
+    // the double-float mixed form's per-tile partial sums [3][nb][npad]
+    // (FP32): entry (c, K, i) is component c of sphere i's acceleration terms
+    // from the partners in 32-sphere block K
     float* f_part;
+    // the FP64-accumulating mixed form's per-tile partial sums [3][nb][npad]
+    // (FP64): entry (c, K, i) is component c of the force on sphere i from
+    // the partners in 32-sphere block K
+    double* part64;
     // mixed form: the pair kernel's tile counter, and per sphere a flag set
     // when any of its pairs is in contact (both zeroed by the drift kernel)
     int* tile_counter;

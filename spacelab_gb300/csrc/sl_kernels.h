@@ -49,7 +49,11 @@ void launch_rowsum_tma(const System& s, const CUtensorMap& map, int b0, int b1, 
                        cudaStream_t st);
 // Status bit set by a kernel whose bounded wait for a TMA copy ran out.
 constexpr unsigned kStatusWaitTimeoutBit = 2u;
+// The double-float mixed form (SL_MODE_MIXED_DF, sl_step_mixed.cu).
 void launch_step_mixed(const System& s, bool write, int num_sms, cudaStream_t st, StepTimers* tm);
+// The mixed form with FP64 displacements, overlaps and accumulation
+// (SL_MODE_MIXED, sl_step_mixed64.cu).
+void launch_step_mixed64(const System& s, bool write, int num_sms, cudaStream_t st, StepTimers* tm);
 // Whether the mixed pair kernel takes two column blocks per item (mixed_pair_items)
 // for nb row blocks on num_sms SMs: where each warp takes many items.
 bool mixed_pair_double(int nb, int num_sms);

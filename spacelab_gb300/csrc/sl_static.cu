@@ -12,6 +12,8 @@
 #include "sl_device.cuh"
 #include "sl_kernels.h"
 
+#include <cuda.h>  // CUcontext, for the driver entry points below
+
 #include <cmath>
 #include <cstdint>
 #include <mutex>
@@ -47,13 +49,54 @@ constexpr size_t kScratchDoubles = kOffScalars + 32;
 __device__ __align__(256) double g_static_scratch[kScratchDoubles];
 
 constexpr int kMaxDevices = 64;
-std::mutex g_mutex;
-double* g_scratch[kMaxDevices] = {};
-int g_num_sms[kMaxDevices] = {};
+// A real sphere's R, m or moi is not finite and > 0 (set by the load kernel).
+constexpr unsigned kStatusBadInputBit = 0x80000000u;
 
-// Device address of g_static_scratch on the current device, looked up once
-// per device.  Host code may not use the symbol itself as a pointer: on the
-// host it names a stand-in object, not device memory.
+struct DeviceSlot {
+    double* scratch = nullptr;
+    int num_sms = 0;
+    unsigned long long ctx_id = 0;  // context the address belongs to (0 = none yet)
+};
+std::mutex g_mutex;
+DeviceSlot g_slots[kMaxDevices];
+
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+// Unique id of the context current on this thread (0 if none is current or
+// the driver does not offer the query).  Ids are never reused within a
+// process, so a context rebuilt by cudaDeviceReset gets a new one.
+unsigned long long current_context_id()
+{
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<CtxGetCurrentFn>(fn);
+        fn = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<CtxGetIdFn>(fn);
+    });
+    if (!get_current || !get_id) return 0;
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (get_current(&ctx) != CUDA_SUCCESS || !ctx) return 0;
+    if (get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
+
+// Device address of g_static_scratch in the current device's current
+// context.  It is looked up (cudaGetSymbolAddress) once per device and
+// looked up again whenever the current context is not the one the cached
+// address came from: after cudaDeviceReset the primary context and its copy
+// of the array are rebuilt, and a driver-API context of its own holds
+// another copy.  Host code may not use the symbol itself as a pointer: on
+// the host it names a stand-in object, not device memory.
 int scratch_for_current_device(double** base, int* num_sms)
 {
     int dev = 0;
@@ -61,7 +104,9 @@ int scratch_for_current_device(double** base, int* num_sms)
     if (e != cudaSuccess) return sl_record_error(SL_ERR_CUDA, cudaGetErrorString(e));
     if (dev < 0 || dev >= kMaxDevices) return sl_record_error(SL_ERR_UNSUPPORTED, "device index out of range");
     std::lock_guard<std::mutex> lock(g_mutex);
-    if (!g_scratch[dev]) {
+    DeviceSlot& slot = g_slots[dev];
+    const unsigned long long ctx = current_context_id();
+    if (!slot.scratch || ctx == 0 || ctx != slot.ctx_id) {
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_static_scratch);
         if (e != cudaSuccess || !p)
@@ -69,11 +114,13 @@ int scratch_for_current_device(double** base, int* num_sms)
         int sms = 0;
         e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (e != cudaSuccess) return sl_record_error(SL_ERR_CUDA, cudaGetErrorString(e));
-        g_scratch[dev] = static_cast<double*>(p);
-        g_num_sms[dev] = sms;
+        slot.scratch = static_cast<double*>(p);
+        slot.num_sms = sms;
+        // the lookup made the runtime's context current if none was
+        slot.ctx_id = ctx ? ctx : current_context_id();
     }
-    *base = g_scratch[dev];
-    *num_sms = g_num_sms[dev];
+    *base = slot.scratch;
+    *num_sms = slot.num_sms;
     return SL_OK;
 }
 
@@ -106,15 +153,17 @@ sl::System static_system(double* base, int n, const sl_material& mat)
 }
 
 // Caller's vec3[n] device arrays -> the scratch's SoA rows; R/m/moi with
-// padding 1; acc/aacc and the error word cleared (the scratch keeps the
-// previous call's contents); scalars dt = 0 (a force pass), kin, kout.
+// padding 1; acc/aacc cleared (the scratch keeps the previous call's
+// contents; the error word is cleared before this kernel runs); scalars
+// dt = 0 (a force pass), kin, kout.
+// A real sphere whose R, m or moi is not finite and > 0 sets
+// kStatusBadInputBit, as sl_upload rejects such values on the handle path.
 __global__ void static_load_kernel(const __grid_constant__ sl::System s, const double* pos, const double* vel,
                                    const double* w, const double* R, const double* m, const double* moi,
                                    double kin, double kout)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) {
-        *s.status = 0u;
         sl::Scalars* sc = const_cast<sl::Scalars*>(s.sc);
         sc->dt = 0.0;
         sc->kin = kin;
@@ -129,9 +178,16 @@ __global__ void static_load_kernel(const __grid_constant__ sl::System s, const d
         s.acc.c[c][i] = 0.0;
         s.aacc.c[c][i] = 0.0;
     }
-    s.R[i] = real ? R[i] : 1.0;
-    s.m[i] = real ? m[i] : 1.0;
-    s.moi[i] = real ? moi[i] : 1.0;
+    double r = real ? R[i] : 1.0, mi = real ? m[i] : 1.0, mo = real ? moi[i] : 1.0;
+    // written so that NaN fails too; a rejected sphere is given 1.0 so that
+    // the rest of the pass runs on ordinary numbers before the call fails
+    if (!(r > 0.0 && r < INFINITY) || !(mi > 0.0 && mi < INFINITY) || !(mo > 0.0 && mo < INFINITY)) {
+        atomicOr(s.status, kStatusBadInputBit);
+        r = mi = mo = 1.0;
+    }
+    s.R[i] = r;
+    s.m[i] = mi;
+    s.moi[i] = mo;
 }
 
 __global__ void static_store_kernel(const __grid_constant__ sl::System s, double* acc, double* aacc,
@@ -166,16 +222,22 @@ extern "C" int sl_forces_static(int n, const double* pos, const double* vel, con
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const sl::System s = static_system(base, n, *mat);
     const int threads = 128;
+    cudaError_t e = cudaMemsetAsync(s.status, 0, sizeof(unsigned int), st);
+    if (e != cudaSuccess) return sl_record_error(SL_ERR_CUDA, cudaGetErrorString(e));
     static_load_kernel<<<(s.npad + threads - 1) / threads, threads, 0, st>>>(s, pos, vel, w, R, m, moi, kin, kout);
     sl::launch_derive(s, st);
     sl::launch_step(s, true, num_sms, st, nullptr);
     static_store_kernel<<<(s.npad + threads - 1) / threads, threads, 0, st>>>(s, acc, aacc, energy);
-    cudaError_t e = cudaGetLastError();
+    e = cudaGetLastError();
     if (e != cudaSuccess) return sl_record_error(SL_ERR_CUDA, cudaGetErrorString(e));
     unsigned int status = 0;
     e = cudaMemcpyAsync(&status, s.status, sizeof(status), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return sl_record_error(SL_ERR_CUDA, cudaGetErrorString(e));
+    if (status & kStatusBadInputBit)
+        return sl_record_error(SL_ERR_ARG, "sl_forces_static: a radius, mass or moment of inertia is not finite and > 0");
+    if (status & sl::kStatusWaitTimeoutBit)
+        return sl_record_error(SL_ERR_TIMEOUT, "sl_forces_static: a bounded wait for asynchronous copies ran out");
     if (status) return sl_record_error(SL_ERR_NONFINITE, "sl_forces_static: non-finite forces or state");
     return SL_OK;
 }

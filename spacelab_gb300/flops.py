@@ -62,3 +62,11 @@ def pair_flops(pairs: int, contacts: int, write: bool = False) -> float:
 #   row sums:    loads those 48 B per unordered pair (24 B per ordered pair)
 PAIR_TERM_BYTES_WRITE = 48
 PAIR_TERM_BYTES_READ = 48
+
+
+# The FP64 work per pair of the mixed form with FP64 geometry and
+# accumulation (SL_MODE_MIXED, sl_step_mixed64.cu), which bounds it: the
+# subtraction pos[B] - pos[A] (3 adds) and the two spheres' FP64 force sums
+# (3 + 3 adds).  Close pairs add their FP64 |r|^2, gap, sqrt and overlap,
+# O(N) of the O(N^2) pairs.
+MIXED64_FP64_OPS_PER_PAIR = 9

@@ -60,7 +60,7 @@ def outcome(c: B.Collision, pos: np.ndarray, e_first: np.ndarray, e_last: np.nda
     return np.array([sf.value, lf.value, rg.value / configs.RADIUS, diss])
 
 
-def simulate(cols: list[B.Collision], steps: int, mode: str = "mixed", skip: int | None = None,
+def simulate(cols: list[B.Collision], steps: int, mode: str = "mixed_df", skip: int | None = None,
              autotune: bool = True) -> tuple[np.ndarray, dict]:
     """Run the collisions through the batched solver; returns (outcomes, info)."""
     skip = steps if skip is None else skip

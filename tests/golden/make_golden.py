@@ -7,7 +7,7 @@ checkpoint steps, the energy totals of every write step and the step-0
 contact set.  Needs the reference tree (for building the pin); the fixtures
 it writes are what the tests use everywhere else.
 
-    make -C oracle REF=/root/reference && python tests/golden/make_golden.py
+    make -C oracle REF=<root of the reference tree> && python tests/golden/make_golden.py
 """
 from __future__ import annotations
 

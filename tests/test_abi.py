@@ -39,7 +39,7 @@ def test_binding_covers_all_declared():
 
 def test_version_and_null_handling():
     lib = _lib.lib()
-    assert lib.sl_version() == 1
+    assert lib.sl_version() == _lib.API_VERSION
     assert lib.sl_destroy(None) == _lib.SL_OK
     assert lib.sl_step(None, 1, 0, None) == _lib.SL_ERR_ARG
     assert b"null" in lib.sl_last_error()

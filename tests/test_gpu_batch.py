@@ -94,7 +94,7 @@ def test_mixed_batch_tracks_exact_batch(shape):
     blocks, contacts in the reference's orientation)."""
     cols = _instances()
     ex = B.BatchRun(cols, "exact", steps=40, skip=10)
-    mx = B.BatchRun(cols, "mixed", steps=40, skip=10)
+    mx = B.BatchRun(cols, "mixed_df", steps=40, skip=10)
     mx.set_shape(*shape)
     ex.run(1, 40, True)
     mx.run(1, 40, True)
@@ -114,7 +114,7 @@ def test_mixed_batch_tracks_exact_batch(shape):
 
 def test_mixed_batch_autotuner_includes_pair_tiles():
     cols = _instances()
-    run = B.BatchRun(cols, "mixed", steps=10, skip=5)
+    run = B.BatchRun(cols, "mixed_df", steps=10, skip=5)
     tuned = run.autotune(sample_steps=2)
     assert len(tuned["times_ms"]) == 12 and all(t > 0 for t in tuned["times_ms"].values())
     assert tuned["tile"] in (0, 32, 64, 128)

@@ -247,9 +247,10 @@ def test_pipelined_step_matches_sequential(n):
         assert np.array_equal(sa[key], sb[key]), key
 
 
-def test_mixed_mode_has_no_pipelined_step():
+@pytest.mark.parametrize("mode", ["mixed", "mixed_df"])
+def test_mixed_mode_has_no_pipelined_step(mode):
     c = contact_case(64, 5)
-    s = _gpu(c, "mixed")
+    s = _gpu(c, mode)
     s.set_overlap(False)
     with pytest.raises(SpaceLabError):
         s.set_overlap(True)

@@ -85,7 +85,7 @@ def test_screened_sweep_gains_over_simulating_every_point():
     the outcomes' own spread (it predicts, not just averages)."""
     steps = 600
     train = B.sample_collisions(384, seed=11, nt_range=(16, 40), clearance=W.CLEARANCE, k_speed_div=W.K_SPEED_DIV)
-    y, info = W.simulate(train, steps, mode="mixed")
+    y, info = W.simulate(train, steps, mode="mixed_df")
     assert info["nonfinite"] == 0
     x = W.features(train)
     ens = S.Ensemble(8, 4, members=5, seed=9)

@@ -13,6 +13,8 @@ This file is collected last (tests/test_zz_*), so a run that stops at the
 first failure has already run every other test.
 """
 import ctypes
+import re
+from pathlib import Path
 
 import numpy as np
 import pytest
@@ -21,6 +23,15 @@ from cases import contact_case, material
 from spacelab_gb300 import BallGroup, GpuStep, _lib
 
 pytestmark = pytest.mark.gpu
+
+HEADER = Path(__file__).resolve().parents[1] / "include" / "spacelab_gpu.h"
+
+
+def _capacity() -> int:
+    """SL_STATIC_MAX_SPHERES as the public header states it."""
+    m = re.search(r"#define\s+SL_STATIC_MAX_SPHERES\s+(\d+)", HEADER.read_text())
+    assert m, "SL_STATIC_MAX_SPHERES not found in spacelab_gpu.h"
+    return int(m.group(1))
 
 
 def _handle_reference(c):
@@ -32,7 +43,7 @@ def _handle_reference(c):
         return g.acc.copy(), g.aacc.copy(), e.as_array()
 
 
-def _static_call(torch, c):
+def _static_call(torch, c, with_energy=True, expect=None):
     lib = _lib.lib()
     n = len(c["R"])
     dev = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64).reshape(-1)).cuda()  # noqa: E731
@@ -43,9 +54,13 @@ def _static_call(torch, c):
     stream = torch.cuda.current_stream().cuda_stream
     mat = material()
     rc = lib.sl_forces_static(n, *[t.data_ptr() for t in ins], ctypes.byref(mat), c["kin"], c["kout"],
-                              acc.data_ptr(), aacc.data_ptr(), energy.data_ptr(), stream)
+                              acc.data_ptr(), aacc.data_ptr(), energy.data_ptr() if with_energy else None, stream)
+    if expect is not None:
+        assert rc == expect, (rc, lib.sl_last_error())
+        return None
     assert rc == _lib.SL_OK, lib.sl_last_error()
-    return acc.cpu().numpy().reshape(-1, 3), aacc.cpu().numpy().reshape(-1, 3), energy.cpu().numpy()
+    e = energy.cpu().numpy() if with_energy else None
+    return acc.cpu().numpy().reshape(-1, 3), aacc.cpu().numpy().reshape(-1, 3), e
 
 
 def _assert_energy_close(e, ref, c, acc_state=None):
@@ -71,10 +86,42 @@ def test_static_force_pass_matches_handle_entry_point_twice():
         _assert_energy_close(e, re, c)
 
 
+def test_static_force_pass_at_capacity_single_sphere_and_without_energy():
+    """n = capacity fills the pair and torque buffers exactly; n = 1 is one
+    pair block with no pairs; energy = NULL skips the totals."""
+    torch = pytest.importorskip("torch")
+    cap = _capacity()
+    for c, with_energy in ((contact_case(cap, 5151), True), (contact_case(1, 5252), True),
+                           (contact_case(150, 5353), False)):
+        acc, aacc, e = _static_call(torch, c, with_energy=with_energy)
+        racc, raacc, re = _handle_reference(c)
+        assert np.array_equal(acc, racc)
+        assert np.array_equal(aacc, raacc)
+        if with_energy:
+            _assert_energy_close(e, re, c)
+
+
+def test_static_force_pass_rejects_bad_sphere_constants():
+    """A zero radius or a NaN mass is refused with SL_ERR_ARG (the handle
+    path refuses them at upload), and the next good call is unaffected."""
+    torch = pytest.importorskip("torch")
+    lib = _lib.lib()
+    for key, idx, val in (("R", 3, 0.0), ("m", 10, float("nan")), ("moi", 0, -1.0)):
+        c = contact_case(40, 5454)
+        c[key] = c[key].copy()
+        c[key][idx] = val
+        _static_call(torch, c, expect=_lib.SL_ERR_ARG)
+        assert b"not finite and > 0" in lib.sl_last_error()
+    c = contact_case(40, 5454)
+    acc, aacc, _ = _static_call(torch, c)
+    racc, raacc, _ = _handle_reference(c)
+    assert np.array_equal(acc, racc) and np.array_equal(aacc, raacc)
+
+
 def test_static_force_pass_rejects_sizes_beyond_capacity():
     lib = _lib.lib()
     mat = material()
-    cap = 256
+    cap = _capacity()
     for n in (0, cap + 1):
         rc = lib.sl_forces_static(n, *([None] * 6), ctypes.byref(mat), 1.0, 0.5, None, None, None, None)
         assert rc == _lib.SL_ERR_ARG
