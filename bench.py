@@ -595,7 +595,9 @@ def run_drift(args) -> dict:
 def run_batched(args) -> dict:
     """Collisions/s of the batched solver (one persistent launch over the
     whole sweep, autotuned shape) next to the same kind of collisions run
-    one at a time through the single-system step."""
+    one at a time through the single-system step: a size-stratified sample
+    of --baseline-instances collisions (evenly spaced quantiles of the
+    sphere count), scaled to the whole sweep."""
     import torch
     from spacelab_gb300 import batch as B
     torch.cuda.init()
@@ -612,35 +614,44 @@ def run_batched(args) -> dict:
     ev1.record()
     torch.cuda.synchronize()
     bad = int(run.status().sum())
+    touched = B.made_contact(run.energy())
     counts = np.array([c.n for c in cols])
     pair_evals = float((counts.astype(np.float64) * (counts - 1) / 2).sum()) * steps
-    k = min(len(cols), args.baseline_instances)
-    base_s, _ = B.run_per_instance(cols[:k], steps, 100, args.mode)
+    idx = B.stratified_indices(cols, args.baseline_instances)
+    sample = [cols[i] for i in idx]
+    k = len(sample)
+    base_s, _ = B.run_per_instance(sample, steps, 100, args.mode)
     base_rate = k / base_s
-    step_s = B.run_per_instance_steps(cols[:k], steps, 100, args.mode)
+    step_s = B.run_per_instance_steps(sample, steps, 100, args.mode)
     step_rate = k / step_s
     rate = len(cols) / wall
+    how = (f"{k} collisions at evenly spaced quantiles of the sphere count ({int(counts[idx].min())}-"
+           f"{int(counts[idx].max())} spheres, {int(touched[idx].sum())} of them made contact), one after another")
     return {"metric": f"batched collisions/s ({len(cols)} collisions, {steps} steps each, {args.mode})",
             "value": rate, "unit": "collisions/s", "higher_is_better": True, "impl": "ours",
             "collisions": len(cols), "steps_per_collision": steps, "spheres_total": int(counts.sum()),
             "spheres_per_collision": [int(counts.min()), int(counts.max())],
+            "collisions_with_contact": int(touched.sum()),
+            "contact_criterion": "E = PE + KE fell by more than 1e-3 of the initial KE (dissipation needs contact)",
             "wall_s": wall, "pair_interactions_per_s": pair_evals / wall, "nonfinite_instances": bad,
             "autotune": tuned,
             "per_instance_baseline": {"collisions": k, "seconds": base_s, "collisions_per_s": base_rate,
-                                      "how": "sl_run per instance (graph per write interval)"},
+                                      "how": how + ", sl_run per instance (graph per write interval)"},
             "per_step_launch_baseline": {"collisions": k, "seconds": step_s, "collisions_per_s": step_rate,
-                                         "how": "sl_step(1) per step per instance (sim_one_step drop-in)"},
+                                         "how": how + ", sl_step(1) per step (the sim_one_step drop-in)"},
             "speedup_over_per_instance": rate / base_rate, "speedup_over_per_step_launches": rate / step_rate,
-            "build_s": build_s,
+            "build_s": build_s, "k_speed_div": 50.0,
             "dtype": "f64" if args.mode == "exact" else "f32+f64",
             "data": "synthetic (seeded collision sweep; no dataset)"}
 
 
 # -------------------------------------------------------- surrogate study --
 def run_surrogate_study(args) -> dict:
-    """Train the 5-member BF16 MLP ensemble on collisions simulated by the
-    batched solver, screen a parameter sweep, re-run uncertain points plus a
-    random audit with the FP64 method, and account the cost."""
+    """Train the 5-member BF16 MLP ensemble on collisions of the batched
+    solver's sweep, choose the screening threshold on held-out validation
+    collisions for a stated error target, screen a parameter sweep, re-run
+    uncertain points plus a random audit with the simulator, and account
+    the cost."""
     import torch
     from spacelab_gb300 import batch as B
     from spacelab_gb300 import surrogate as S
@@ -648,24 +659,38 @@ def run_surrogate_study(args) -> dict:
     torch.cuda.init()
     steps = args.study_steps
     t0 = time.perf_counter()
-    train = B.sample_collisions(args.train_collisions, seed=21, nt_range=W.NT_RANGE, clearance=W.CLEARANCE,
-                                k_speed_div=W.K_SPEED_DIV)
+    data = B.sample_collisions(args.train_collisions, seed=21, nt_range=W.NT_RANGE, clearance=W.CLEARANCE,
+                               k_speed_div=W.K_SPEED_DIV)
     build_s = time.perf_counter() - t0
-    y, sim_info = W.simulate(train, steps, mode="mixed_df")
-    x = W.features(train)
+    y, sim_info = W.simulate(data, steps, mode="mixed_df")
+    x = W.features(data)
+    perm = np.random.default_rng(24).permutation(len(data))
+    nval = max(1, len(data) // 10)
+    val, trn = perm[:nval], perm[nval:]
     ens = S.Ensemble(8, 4, members=5, seed=3)
-    fit = ens.fit(x, y, epochs=args.epochs, batch=256, lr=1e-3)
+    fit = ens.fit(x[trn], y[trn], epochs=args.epochs, batch=256, lr=1e-3)
+    targets = sorted({0.15, 0.2, 0.25, 0.3, 0.4, args.error_target})
+    curve = {str(t): W.pick_threshold(ens, x[val], y[val], t) for t in targets}
+    chosen = curve[str(args.error_target)]
     points = W.sample_params(args.sweep_points, seed=22)
-    res = W.screen_sweep(ens, points, steps, threshold=args.threshold, audit=args.audit, seed=23, sim_mode="exact",
-                         max_uncertain=args.max_uncertain)
-    mean_pred = np.abs(y.mean(0) - y).mean(0)  # the method without the network: predict the training mean
-    return {"metric": "surrogate-screened sweep cost ratio (full FP64 simulation / screened)",
+    res = W.screen_sweep(ens, points, steps, threshold=chosen["threshold"], audit=args.audit, seed=23,
+                         sim_mode="mixed_df", fp64_check=args.fp64_check)
+    # the method without the network: predict the training mean everywhere
+    mean_pred = (np.abs(y[trn].mean(0) - y[val]).mean(0) / ens.ys).tolist()
+    return {"metric": "surrogate-screened sweep cost ratio (simulating every point / screened)",
             "value": res["cost_ratio"], "unit": "x", "higher_is_better": True,
-            "train_collisions": len(train), "steps_per_collision": steps, "train_sim_s": sim_info["seconds"],
-            "train_sim_pairs_per_s": sim_info["pair_evals"] / sim_info["seconds"], "build_s": build_s,
+            "outcome_error": f"mean absolute error of accepted validation points <= {args.error_target} x each "
+                             f"outcome's spread",
+            "train_collisions": len(trn), "validation_collisions": len(val), "steps_per_collision": steps,
+            "train_sim_s": sim_info["seconds"], "train_sim_pairs_per_s": sim_info["pair_evals"] / sim_info["seconds"],
+            "train_nonfinite": sim_info["nonfinite"], "build_s": build_s,
             "fit_s": fit["seconds"], "final_loss": fit["final_loss"], "outcomes": list(S.OUTCOMES),
-            "outcome_mean_abs_dev": mean_pred.tolist(), "screen": res,
-            "recipe": {"nt_range": list(W.NT_RANGE), "clearance_radii": W.CLEARANCE, "k_speed_div": W.K_SPEED_DIV},
+            "outcome_spread": ens.ys.tolist(),
+            "threshold_by_validation": curve, "chosen": chosen,
+            "validation_mae_std_units_without_network": mean_pred,
+            "screen": res,
+            "recipe": {"nt_range": list(W.NT_RANGE), "clearance": "centres 1.1 (Rt+Rp) apart",
+                       "k_speed_div": W.K_SPEED_DIV, "simulator": "batched solver, mixed_df"},
             "data": "synthetic (seeded collision sweep; no dataset)"}
 
 
@@ -737,17 +762,19 @@ def main(argv=None) -> int:
     ap.add_argument("--batched", type=int, default=0,
                     help="instead of the benchmark: this many sampled collisions through the batched solver")
     ap.add_argument("--batch-steps", type=int, default=300)
-    ap.add_argument("--baseline-instances", type=int, default=16)
+    ap.add_argument("--baseline-instances", type=int, default=64)
     ap.add_argument("--surrogate-study", action="store_true",
                     help="instead of the benchmark: train the surrogate ensemble and screen a sweep")
     ap.add_argument("--train-collisions", type=int, default=50000)
-    ap.add_argument("--sweep-points", type=int, default=100000)
-    ap.add_argument("--study-steps", type=int, default=4000)
+    ap.add_argument("--sweep-points", type=int, default=1000000)
+    ap.add_argument("--study-steps", type=int, default=3000)
     ap.add_argument("--epochs", type=int, default=150)
-    ap.add_argument("--threshold", type=float, default=0.3)
+    ap.add_argument("--error-target", type=float, default=0.25,
+                    help="surrogate study: mean absolute error of the accepted validation points, in units of "
+                         "each outcome's spread, that sets the screening threshold")
     ap.add_argument("--audit", type=float, default=0.01)
-    ap.add_argument("--max-uncertain", type=float, default=0.03,
-                    help="re-run at most this fraction of the sweep as uncertain (raises the threshold)")
+    ap.add_argument("--fp64-check", type=int, default=64,
+                    help="surrogate study: audit points also re-run with the FP64 exact method")
     ap.add_argument("--nt-min", type=int, default=64)
     ap.add_argument("--nt-max", type=int, default=1600)
     args = ap.parse_args(argv)

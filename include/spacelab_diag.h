@@ -6,6 +6,8 @@
 #ifndef SPACELAB_DIAG_H
 #define SPACELAB_DIAG_H
 
+#include <stdint.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -41,6 +43,15 @@ int sl_diag_fp64_peak(double* gflops);
 
 /* The same for FP32 fused multiply-adds (the mixed form's pipe). */
 int sl_diag_fp32_peak(double* gflops);
+
+/* One surrogate GEMM on host data, for checking the GEMM kernels:
+ * C[M][N] = A[M][K] . B[N][K]^T (+ bias[N]) with A, B bf16 bit patterns,
+ * row-major; C f32 [M][N]; Cb (may be NULL) gets bf16(act ? GELU(C) : C).
+ * kernel 0: the mma.sync kernel (K a multiple of 32); 1: the tcgen05 kernel
+ * (K a multiple of 8).  Allocates its own device buffers.  No counterpart in
+ * the reference. */
+int sl_diag_gemm_bf16(int M, int N, int K, const uint16_t* A, const uint16_t* B, const float* bias, int act,
+                      int kernel, float* C, uint16_t* Cb);
 
 #ifdef __cplusplus
 }

@@ -42,6 +42,17 @@ int slh_build_collision(int n_t, int n_p, double radius, double rho, double phi,
                         double speed, double off_x, double off_y, uint64_t seed_t, uint64_t seed_p,
                         double* pos, double* vel, double* w, double* R, double* m, double* moi);
 
+/* Radii of gyration of `count` monodisperse clusters, each built exactly as
+ * slh_build_collision builds its target and its projectile (slh_build_cluster
+ * with sigma_ln = 0 and the velocity spread 1e-3 cm/s, which does not move
+ * the spheres): cluster k has n[k] spheres of `radius` from seed[k].  rg[k]
+ * gets its radius of gyration (-1 if it could not be built).  `threads` host
+ * threads (< 1: all).  No counterpart in the reference: it gives a
+ * collision sweep its clusters' measured radii of gyration without keeping
+ * the clusters.  Returns 0, 1 on bad arguments, 2 if a cluster failed. */
+int slh_cluster_rg(int count, const int* n, const uint64_t* seed, double radius, double rho, double phi,
+                   int threads, double* rg);
+
 /* Spring constants and time step: kin = kConsts r_max v^2 with
  * kConsts = 3e3 (4/3 pi rho) / maxOverlap^2, maxOverlap = 0.1
  * (ball_group.hpp:1316, dust_const.hpp:30-35); kout = cor kin

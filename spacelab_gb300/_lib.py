@@ -109,9 +109,12 @@ _PROTOS = [
     ("sl_diag_division", ctypes.c_int, [ctypes.c_int] + [_c_double_p] * 4),
     ("sl_diag_fp64_peak", ctypes.c_int, [_c_double_p]),
     ("sl_diag_fp32_peak", ctypes.c_int, [_c_double_p]),
+    ("sl_diag_gemm_bf16", ctypes.c_int, [ctypes.c_int] * 3 + [ctypes.POINTER(ctypes.c_uint16)] * 2 +
+     [ctypes.POINTER(ctypes.c_float), ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_float),
+      ctypes.POINTER(ctypes.c_uint16)]),
     ("sl_diag_fp64_add_latency", ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     ("sl_diag_exact_ops", ctypes.c_int, [ctypes.c_int] + [_c_double_p] * 3),
-("sl_diag_int_ops", ctypes.c_int, [ctypes.c_int] + [_c_double_p] * 3),
+    ("sl_diag_int_ops", ctypes.c_int, [ctypes.c_int] + [_c_double_p] * 3),
     # host setup (spacelab_host.h)
     ("slh_build_cluster", ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                          ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
@@ -121,6 +124,8 @@ _PROTOS = [
                                            ctypes.c_double, ctypes.c_uint64, ctypes.c_uint64] + [_c_double_p] * 6),
     ("slh_spring_and_dt", ctypes.c_int, [ctypes.c_double] * 6 + [_c_double_p] * 3),
     ("slh_to_origin", ctypes.c_int, [ctypes.c_int, _c_double_p, _c_double_p]),
+    ("slh_cluster_rg", ctypes.c_int, [ctypes.c_int, _c_int_p, ctypes.POINTER(ctypes.c_uint64), ctypes.c_double,
+                                      ctypes.c_double, ctypes.c_double, ctypes.c_int, _c_double_p]),
     ("slh_write_simdata_header", ctypes.c_int, [ctypes.c_char_p, ctypes.c_int]),
     ("slh_append_simdata_row", ctypes.c_int, [ctypes.c_char_p, ctypes.c_int] + [_c_double_p] * 3 + [ctypes.c_int]),
     ("slh_write_energy_header", ctypes.c_int, [ctypes.c_char_p]),

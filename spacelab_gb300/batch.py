@@ -12,8 +12,12 @@
 Each instance is built like the N=5000 aggregate collision: two seeded
 clusters, the projectile 1.1 (R_t + R_p) away along x and b along y, opposite
 kicks to zero momentum, target first, centre of mass at the origin. Its k
-comes from the reference's formula at one tenth of the impact speed, and
-dt = contact time / 50.
+comes from the reference's formula at 1/50 of the impact speed (as the
+N=5000 collision's 2 cm/s for 100 cm/s), and dt = contact time / 50.  The
+projectile then travels ~12 radii in 3000 steps at any speed (dt scales as
+1/speed), enough to reach the target from 1.1 (R_t + R_p), and a head-on
+impact overlaps ~9% of a radius, below the reference's design overlap of
+10% (maxOverlap, dust_const.hpp:31).
 
 ``BatchRun`` advances all instances in one persistent launch; ``run_per_instance``
 is the comparison: the same instances one after another through the
@@ -54,7 +58,7 @@ class Collision:
 
 def sample_collisions(count: int, seed: int, nt_range=(64, 1600), speed_range=(10.0, 1000.0), cor_range=(0.4, 0.8),
                       mu_range=(0.1, 0.5), build: bool = True, clearance: float | None = None,
-                      k_speed_div: float = 10.0) -> list[Collision]:
+                      k_speed_div: float = 50.0) -> list[Collision]:
     rng = np.random.default_rng(seed)
     out = []
     for k in range(count):
@@ -69,7 +73,12 @@ def sample_collisions(count: int, seed: int, nt_range=(64, 1600), speed_range=(1
     return out
 
 
-def build_instance(c: Collision, clearance: float | None = None, k_speed_div: float = 10.0) -> Collision:
+def cluster_seeds(c: Collision) -> tuple[int, int]:
+    """Seeds of the target's and the projectile's cluster."""
+    return c.seed, c.seed ^ 0x5DEECE66D
+
+
+def build_instance(c: Collision, clearance: float | None = None, k_speed_div: float = 50.0) -> Collision:
     """Build the two clusters.  clearance None: centres 1.1 (R_t + R_p) apart
     along x; otherwise the bounding spheres are `clearance` sphere radii
     apart.  k from the reference formula at speed / k_speed_div."""
@@ -79,7 +88,8 @@ def build_instance(c: Collision, clearance: float | None = None, k_speed_div: fl
         rt = configs.RADIUS * (c.n_t / configs.PHI) ** (1 / 3)
         rp = configs.RADIUS * (c.n_p / configs.PHI) ** (1 / 3)
         off_x = 1.0 + clearance * configs.RADIUS / (rt + rp)
-    g = configs.build_collision(c.n_t, c.n_p, c.speed, off_x, c.b_frac, c.seed, c.seed ^ 0x5DEECE66D)
+    seed_t, seed_p = cluster_seeds(c)
+    g = configs.build_collision(c.n_t, c.n_p, c.speed, off_x, c.b_frac, seed_t, seed_p)
     kin, kout, dt = configs.spring_and_dt(float(g.R.max()), float(g.m.min()), c.speed / k_speed_div,
                                           cor=c.cor * c.cor)
     c.group, c.kin, c.kout, c.dt = g, kin, kout, dt
@@ -175,6 +185,26 @@ class BatchRun:
         s = np.zeros(len(self.cols), dtype=np.uint32)
         check(self.lib.sl_batch_status(self.h, s.ctypes.data_as(ctypes.POINTER(ctypes.c_uint))), "sl_batch_status")
         return s
+
+
+def stratified_indices(cols: list[Collision], k: int) -> np.ndarray:
+    """k collisions at evenly spaced quantiles of the sphere count (the
+    middle of k equal-count strata of the size-sorted sweep), so that a
+    per-instance baseline timed on them and scaled by len(cols) / k
+    estimates the whole sweep's time without size bias."""
+    order = np.argsort([c.n for c in cols], kind="stable")
+    k = min(k, len(cols))
+    pick = ((np.arange(k) + 0.5) * len(cols) / k).astype(int)
+    return order[pick]
+
+
+def made_contact(energy: np.ndarray, frac: float = 1e-3) -> np.ndarray:
+    """Per instance, whether its clusters touched: restitution and friction
+    dissipate energy only in contact, so E = PE + KE falling by more than
+    `frac` of the initial kinetic energy marks a contact.  energy is
+    [ninst][nrec][8] (BatchRun.energy)."""
+    E = energy[:, :, 0] + energy[:, :, 1]
+    return (E[:, 0] - E[:, -1]) > frac * energy[:, 0, 1]
 
 
 def run_per_instance(cols: list[Collision], steps: int, skip: int, mode: str = "exact") -> tuple[float, list]:

@@ -4,9 +4,11 @@
 #include "../../../include/spacelab_host.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 namespace {
@@ -225,6 +227,41 @@ int slh_build_collision(int n_t, int n_p, double radius, double rho, double phi,
     }
     for (int i = 0; i < n_t; ++i) vel[3 * i] += vBig;
     return slh_to_origin(n, pos, m);
+}
+
+int slh_cluster_rg(int count, const int* n, const uint64_t* seed, double radius, double rho, double phi,
+                   int threads, double* rg)
+{
+    if (count < 0 || (count > 0 && (!n || !seed || !rg)) || !(radius > 0)) return 1;
+    if (threads < 1) threads = (int)std::max(1u, std::thread::hardware_concurrency());
+    threads = std::min(threads, std::max(1, count));
+    std::atomic<int> next{0};
+    std::atomic<int> failed{0};
+    auto work = [&]() {
+        std::vector<double> pos, vel, w, R, m, moi;
+        for (int k = next.fetch_add(1); k < count; k = next.fetch_add(1)) {
+            const int nk = n[k];
+            if (nk < 1) { failed.store(1); rg[k] = -1.0; continue; }
+            pos.resize(3 * (size_t)nk); vel.resize(3 * (size_t)nk); w.resize(3 * (size_t)nk);
+            R.resize(nk); m.resize(nk); moi.resize(nk);
+            // the same call slh_build_collision makes for each of its clusters
+            if (slh_build_cluster(nk, radius, 0, 1, 1, rho, phi, 1e-3, seed[k], pos.data(), vel.data(), w.data(),
+                                  R.data(), m.data(), moi.data())) {
+                failed.store(1);
+                rg[k] = -1.0;
+                continue;
+            }
+            if (slh_radius_of_gyration(nk, pos.data(), m.data(), &rg[k])) {
+                failed.store(1);
+                rg[k] = -1.0;
+            }
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < threads; ++t) pool.emplace_back(work);
+    work();
+    for (auto& t : pool) t.join();
+    return failed.load() ? 2 : 0;
 }
 
 int slh_spring_and_dt(double r_max, double m_min, double speed, double rho, double cor,

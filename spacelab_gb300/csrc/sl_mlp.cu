@@ -18,13 +18,18 @@
 #include "../../include/spacelab_mlp.h"
 #include "../../include/spacelab_gpu.h"
 
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
+
+#include "sl_tma.cuh"
 
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <random>
 #include <string>
@@ -132,6 +137,202 @@ __global__ void __launch_bounds__(128) gemm_nt_kernel(const bf16* __restrict__ A
                     if (Cb) Cb[(size_t)row * ldc + col + e] = __float2bfloat16(act ? gelu(v) : v);
                 }
             }
+}
+
+// ------------------------------------------------------------- tcgen05 --
+// C[M][N] = A[M][K] . B[N][K]^T on the fifth-generation tensor cores.  One
+// CTA (4 warps) per 128-row block of C and BN columns; its accumulator is
+// BN f32 columns x 128 lanes of tensor memory (TMEM).  K is taken in chunks
+// of 64 elements (128 bytes): TMA copies the A and B chunks into shared
+// memory with the 128-byte swizzle -- the K-major layout the MMA's shared-
+// memory descriptors describe (8-row groups 1024 bytes apart) -- into one of
+// two stages, and one thread issues four tcgen05.mma (M=128, N=BN, K=16)
+// per chunk, then tcgen05.commit to the stage's barrier so that the next
+// copy into that stage waits for the MMAs reading it.  Boxes past M, N or K
+// are zero-filled by the copy engine.  The epilogue: warp w reads TMEM
+// lanes 32w..32w+31 (rows m0 + 32w + lane) 32 columns at a time with
+// tcgen05.ld, adds the bias and writes the FP32 and/or BF16 (GELU or
+// identity) outputs.  Every wait is bounded (sl_tma.cuh); a wait that runs
+// out sets *err, the CTA waits (bounded) for its MMAs, frees its TMEM and
+// returns.
+constexpr int kTcM = 128, kTcK = 64, kTcStages = 2;
+constexpr int kTcThreads = 128;
+
+template <int BN>
+struct TcSmem {
+    static constexpr int kABytes = kTcM * kTcK * 2;  // 16 KB
+    static constexpr int kBBytes = BN * kTcK * 2;
+    static constexpr int kBytes = kTcStages * (kABytes + kBBytes) + 1024 /* barriers etc. */ + 1024 /* alignment */;
+};
+
+// Shared-memory matrix descriptor of a K-major tile with the 128-byte
+// swizzle: start address >> 4 (bits 0-13), leading byte offset (unused for
+// this layout; 16 bytes, bits 16-29), stride byte offset 1024 = 8 rows x 128
+// bytes (bits 32-45), descriptor version 1 (bits 46-47), base offset 0 (the
+// tile is 1024-byte aligned), layout SWIZZLE_128B = 2 (bits 61-63).  The
+// K = 16 sub-steps within a 128-byte row advance the start address by 32
+// bytes.
+__device__ __forceinline__ uint64_t tc_desc_sw128(uint32_t saddr)
+{
+    return (uint64_t)((saddr >> 4) & 0x3fffu) | ((uint64_t)(16 >> 4) << 16) | ((uint64_t)(1024 >> 4) << 32) |
+           ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+// Instruction descriptor of kind::f16: D f32 (bits 4-5 = 1), A and B bf16
+// (bits 7-9 and 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 (bits
+// 17-22), M >> 4 (bits 24-28).
+__host__ __device__ constexpr uint32_t tc_idesc_bf16(int M, int N)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, int accumulate)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+        ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+// Arrives on `bar` once every tcgen05.mma this thread issued has completed.
+__device__ __forceinline__ void tc_commit(uint64_t* bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                 ::"r"(sl::tma::smem_addr(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// 32 consecutive f32 columns of this thread's TMEM lane.
+__device__ __forceinline__ void tc_ld32(uint32_t taddr, float* v)
+{
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+template <int BN>
+__global__ void __launch_bounds__(kTcThreads) gemm_nt_tc_kernel(const __grid_constant__ CUtensorMap mapA,
+                                                                 const __grid_constant__ CUtensorMap mapB,
+                                                                 const float* __restrict__ bias, float* Cf, bf16* Cb,
+                                                                 int ldc, int M, int N, int K, int act, int* err)
+{
+    using Sm = TcSmem<BN>;
+    extern __shared__ unsigned char tc_raw[];
+    unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(tc_raw) + 1023) &
+                                                           ~static_cast<uintptr_t>(1023));
+    unsigned char* sa = base;                                  // [stage][128 rows][128 B]
+    unsigned char* sb = base + kTcStages * Sm::kABytes;        // [stage][BN rows][128 B]
+    uint64_t* full = reinterpret_cast<uint64_t*>(sb + kTcStages * Sm::kBBytes);
+    uint64_t* empty = full + kTcStages;
+    uint64_t* done = empty + kTcStages;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+    int* failed = reinterpret_cast<int*>(tmem_slot + 1);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int m0 = blockIdx.y * kTcM, n0 = blockIdx.x * BN;
+    const int nk = (K + kTcK - 1) / kTcK;
+
+    if (tid == 0) {
+        for (int st = 0; st < kTcStages; ++st) {
+            sl::tma::mbar_init(&full[st], 1);
+            sl::tma::mbar_init(&empty[st], 1);
+        }
+        sl::tma::mbar_init(done, 1);
+        *failed = 0;
+        sl::tma::fence_barrier_init();
+    }
+    if (warp == 0) {  // BN f32 columns of TMEM (a power of two >= 32)
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     ::"r"(sl::tma::smem_addr(tmem_slot)), "r"(BN)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (tid == 0) {
+        constexpr uint32_t idesc = tc_idesc_bf16(kTcM, BN);
+        const uint32_t bytes = Sm::kABytes + Sm::kBBytes;
+        auto issue = [&](int kc) {
+            const int st = kc % kTcStages;
+            sl::tma::mbar_arrive_expect_tx(&full[st], bytes);
+            sl::tma::load_2d(sa + st * Sm::kABytes, &mapA, kc * kTcK, m0, &full[st]);
+            sl::tma::load_2d(sb + st * Sm::kBBytes, &mapB, kc * kTcK, n0, &full[st]);
+        };
+        int issued = 0;
+        for (; issued < nk && issued < kTcStages; ++issued) issue(issued);
+        bool ok = true;
+        int kc = 0;
+        for (; kc < nk && ok; ++kc) {
+            const int st = kc % kTcStages;
+            const uint32_t par = (uint32_t)(kc / kTcStages) & 1u;
+            if (!sl::tma::mbar_wait(&full[st], par)) { ok = false; break; }
+            tc_fence_after();
+            const uint32_t a0 = sl::tma::smem_addr(sa + st * Sm::kABytes);
+            const uint32_t b0 = sl::tma::smem_addr(sb + st * Sm::kBBytes);
+#pragma unroll
+            for (int k = 0; k < kTcK / 16; ++k)
+                tc_mma(tmem, tc_desc_sw128(a0 + 32 * k), tc_desc_sw128(b0 + 32 * k), idesc, (kc | k) != 0);
+            tc_commit(&empty[st]);
+            if (kc + kTcStages < nk) {
+                // the stage's next copy waits for the MMAs that read it
+                if (!sl::tma::mbar_wait(&empty[st], par)) { ok = false; ++kc; break; }
+                issue(kc + kTcStages);
+                ++issued;
+            }
+        }
+        tc_commit(done);  // arrives when every MMA issued above has completed
+        if (!ok) {
+            *failed = 1;
+            // let the copies in flight land before the CTA's memory is reused
+            for (int q = kc; q < issued; ++q)
+                sl::tma::mbar_wait(&full[q % kTcStages], (uint32_t)(q / kTcStages) & 1u);
+        }
+    }
+    __syncwarp();
+    const bool mma_done = sl::tma::mbar_wait(done, 0);
+    tc_fence_after();
+    __syncthreads();
+    if (*failed || !mma_done) {
+        if (tid == 0) atomicExch(err, 1);
+    } else {
+        const int row = m0 + warp * 32 + lane;
+#pragma unroll 1
+        for (int cg = 0; cg < BN / 32; ++cg) {
+            float v[32];
+            tc_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(cg * 32), v);
+            if (row < M) {
+#pragma unroll
+                for (int i = 0; i < 32; ++i) {
+                    const int col = n0 + cg * 32 + i;
+                    if (col >= N) break;
+                    const float z = v[i] + (bias ? bias[col] : 0.0f);
+                    if (Cf) Cf[(size_t)row * ldc + col] = z;
+                    if (Cb) Cb[(size_t)row * ldc + col] = __float2bfloat16(act ? gelu(z) : z);
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN) : "memory");
 }
 
 // out[c][r] = in[r][c]
@@ -251,11 +452,80 @@ struct sl_mlp {
 
 namespace {
 
-void gemm(cudaStream_t st, const bf16* A, int lda, const bf16* B, int ldb, const float* bias, float* Cf, bf16* Cb,
-          int ldc, int M, int N, int K, int act)
+void gemm_mma_sync(cudaStream_t st, const bf16* A, int lda, const bf16* B, int ldb, const float* bias, float* Cf,
+                   bf16* Cb, int ldc, int M, int N, int K, int act)
 {
     dim3 grid((N + kTN - 1) / kTN, (M + kTM - 1) / kTM);
     gemm_nt_kernel<<<grid, 128, 0, st>>>(A, lda, B, ldb, bias, Cf, Cb, ldc, M, N, K, act);
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 mlp_map_encoder()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    });
+    return encode;
+}
+
+// A row-major bf16 matrix [rows][k] with leading dimension ld (elements) as a
+// 2D tensor map: boxes of 64 elements (128 bytes) of k x box_rows rows, the
+// 128-byte swizzle, zero fill outside the matrix.
+bool make_tc_map(CUtensorMap* map, const bf16* base, int rows, int k, int ld, int box_rows)
+{
+    PFN_cuTensorMapEncodeTiled_v12000 encode = mlp_map_encoder();
+    if (!encode || !base || (reinterpret_cast<uintptr_t>(base) & 15u) || (ld * 2) % 16) return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)k, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+    const cuuint32_t box[2] = {(cuuint32_t)kTcK, (cuuint32_t)box_rows};
+    const cuuint32_t estr[2] = {1, 1};
+    return encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<bf16*>(base), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int BN>
+bool launch_tc(cudaStream_t st, const CUtensorMap& ma, const bf16* B, int ldb, const float* bias, float* Cf, bf16* Cb,
+               int ldc, int M, int N, int K, int act, int* err)
+{
+    static bool attr_set = false;  // per BN; the attribute is per function
+    if (!attr_set) {
+        if (cudaFuncSetAttribute(gemm_nt_tc_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 TcSmem<BN>::kBytes) != cudaSuccess)
+            return false;
+        attr_set = true;
+    }
+    CUtensorMap mb;
+    if (!make_tc_map(&mb, B, N, K, ldb, BN)) return false;
+    dim3 grid((N + BN - 1) / BN, (M + kTcM - 1) / kTcM);
+    gemm_nt_tc_kernel<BN><<<grid, kTcThreads, TcSmem<BN>::kBytes, st>>>(ma, mb, bias, Cf, Cb, ldc, M, N, K, act, err);
+    return true;
+}
+
+// The tcgen05 GEMM; false if its tensor maps or launch attributes cannot be
+// set up (the caller reports the error; nothing is launched then).
+bool gemm_tc(cudaStream_t st, const bf16* A, int lda, const bf16* B, int ldb, const float* bias, float* Cf, bf16* Cb,
+             int ldc, int M, int N, int K, int act, int* err)
+{
+    CUtensorMap ma;
+    if (!make_tc_map(&ma, A, M, K, lda, kTcM)) return false;
+    // at most 128 columns per CTA: the products are small (M of a few
+    // hundred rows), so more, narrower CTAs spread them over more SMs
+    if (N <= 32) return launch_tc<32>(st, ma, B, ldb, bias, Cf, Cb, ldc, M, N, K, act, err);
+    if (N <= 64) return launch_tc<64>(st, ma, B, ldb, bias, Cf, Cb, ldc, M, N, K, act, err);
+    return launch_tc<128>(st, ma, B, ldb, bias, Cf, Cb, ldc, M, N, K, act, err);
+}
+
+void gemm(cudaStream_t st, const bf16* A, int lda, const bf16* B, int ldb, const float* bias, float* Cf, bf16* Cb,
+          int ldc, int M, int N, int K, int act)
+{
+    gemm_mma_sync(st, A, lda, B, ldb, bias, Cf, Cb, ldc, M, N, K, act);
 }
 
 void transpose(cudaStream_t st, const bf16* in, int rows, int cols, int ldi, bf16* out, int ldo)
@@ -496,3 +766,51 @@ int sl_mlp_predict(sl_mlp* h, const float* x, int n, float* y)
 }
 
 }  // extern "C"
+
+extern "C" int sl_diag_gemm_bf16(int M, int N, int K, const uint16_t* A, const uint16_t* B, const float* bias,
+                                 int act, int kernel, float* C, uint16_t* Cb)
+{
+    if (M < 1 || N < 1 || K < 1 || K % 8 || !A || !B || !C || (kernel != 0 && kernel != 1))
+        return sl_record_error(SL_ERR_ARG, "sl_diag_gemm_bf16: need M, N >= 1, K a multiple of 8, kernel 0 or 1");
+    if (kernel == 0 && K % kTK)
+        return sl_record_error(SL_ERR_ARG, "sl_diag_gemm_bf16: the mma.sync kernel needs K a multiple of 32");
+    const size_t na = (size_t)M * K, nbb = (size_t)N * K, nc = (size_t)M * N;
+    size_t off = 0;
+    auto take = [&](size_t b) { size_t o = off; off = (off + b + 255) / 256 * 256; return o; };
+    const size_t oA = take(na * 2), oB = take(nbb * 2), oBias = take((size_t)N * 4), oC = take(nc * 4),
+                 oCb = take(nc * 2), oErr = take(sizeof(int));
+    void* arena = nullptr;
+    if (cudaMalloc(&arena, off) != cudaSuccess) return sl_record_error(SL_ERR_ALLOC, "sl_diag_gemm_bf16: cudaMalloc");
+    char* b = static_cast<char*>(arena);
+    bf16* dA = (bf16*)(b + oA);
+    bf16* dB = (bf16*)(b + oB);
+    float* dBias = bias ? (float*)(b + oBias) : nullptr;
+    float* dC = (float*)(b + oC);
+    bf16* dCb = Cb ? (bf16*)(b + oCb) : nullptr;
+    int* dErr = (int*)(b + oErr);
+    int rc = SL_OK;
+    cudaMemcpy(dA, A, na * 2, cudaMemcpyHostToDevice);
+    cudaMemcpy(dB, B, nbb * 2, cudaMemcpyHostToDevice);
+    if (bias) cudaMemcpy(dBias, bias, (size_t)N * 4, cudaMemcpyHostToDevice);
+    cudaMemset(dErr, 0, sizeof(int));
+    if (kernel == 0) {
+        gemm_mma_sync(nullptr, dA, K, dB, K, dBias, dC, dCb, N, M, N, K, act);
+    } else if (!gemm_tc(nullptr, dA, K, dB, K, dBias, dC, dCb, N, M, N, K, act, dErr)) {
+        rc = sl_record_error(SL_ERR_CUDA, "sl_diag_gemm_bf16: tensor map or launch setup failed");
+    }
+    if (rc == SL_OK) {
+        cudaError_t e = cudaDeviceSynchronize();
+        if (e != cudaSuccess) rc = sl_record_error(SL_ERR_CUDA, cudaGetErrorString(e));
+    }
+    int herr = 0;
+    if (rc == SL_OK) {
+        cudaMemcpy(&herr, dErr, sizeof(int), cudaMemcpyDeviceToHost);
+        if (herr) rc = sl_record_error(SL_ERR_TIMEOUT, "sl_diag_gemm_bf16: a bounded wait in the tcgen05 GEMM ran out");
+    }
+    if (rc == SL_OK) {
+        cudaMemcpy(C, dC, nc * 4, cudaMemcpyDeviceToHost);
+        if (Cb) cudaMemcpy(Cb, dCb, nc * 2, cudaMemcpyDeviceToHost);
+    }
+    cudaFree(arena);
+    return rc;
+}

@@ -89,6 +89,7 @@ template <bool WRITE>
 __global__ void __launch_bounds__(128, 4) pair_tile_kernel(const __grid_constant__ System s, int c0, int c1)
 {
     __shared__ ABlock sA[4];
+    __shared__ double sB[4][kBStageDoubles];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     ABlock& ab = sA[wib];
@@ -126,10 +127,10 @@ __global__ void __launch_bounds__(128, 4) pair_tile_kernel(const __grid_constant
         const TileUniform tu{R0, twoR0, sum0, c40, P0};
         if (uni)
             tile_pairs<WRITE, true>(s, ab, X, Y, lane, a_end, bx, by, bz, Rb, twoRb, mb, rmb, bvalid, tu, h_min_bits,
-                                    Ha, rowA, rowB, pe, rowbits, colbits);
+                                    Ha, rowA, rowB, pe, rowbits, colbits, sB[wib]);
         else
             tile_pairs<WRITE, false>(s, ab, X, Y, lane, a_end, bx, by, bz, Rb, twoRb, mb, rmb, bvalid, tu, h_min_bits,
-                                     Ha, rowA, rowB, pe, rowbits, colbits);
+                                     Ha, rowA, rowB, pe, rowbits, colbits, sB[wib]);
         // Contact bits: row A = 32X + lane gets block Y's bits, row B gets
         // block X's bits; on the diagonal both describe row 32X + lane.
         if (X == Y) {

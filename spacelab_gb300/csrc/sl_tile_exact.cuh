@@ -23,17 +23,35 @@ struct TileUniform {
     double R0, twoR0, sum0, c40, P0;
 };
 
+// Per-warp shared staging of sphere B's terms (lane = B) for four
+// consecutive partners: [component][lane][4 + 1 padding] doubles, so that a
+// lane's 8-byte accesses at a 40-byte stride fall in distinct banks per
+// half-warp.
+constexpr int kBStageRow = 5;
+constexpr int kBStagePlane = kBlock * kBStageRow;
+constexpr int kBStageDoubles = 3 * kBStagePlane;
+
 // The pairs of one tile (X, Y) for lane = sphere B: terms to pairbuf and
 // torqbuf, contact bits to rowbits/colbits, PE (write steps) to pe.
+// bstage (kBStageDoubles per warp, or NULL): off the diagonal, sphere B's
+// terms -- which go to B's own row of pairbuf, a different row per lane --
+// are gathered four at a time and written as whole 32-byte sectors (two
+// 16-byte stores per component) instead of one 8-byte store per term from
+// 32 rows at once; partners past the last sphere are written as +0.0, the
+// value those entries hold anyway.  On the diagonal tile, and with NULL,
+// every term is stored as it is computed.
 template <bool WRITE, bool UNI>
 __device__ __forceinline__ void tile_pairs(const System& s, const ABlock& ab, int X, int Y, int lane, int a_end,
                                            double bx, double by, double bz, double Rb, double twoRb, double mb,
                                            unsigned long long rmb, bool bvalid, const TileUniform& tu,
                                            long long h_min_bits, double Ha, double* rowA, double* rowB,
-                                           double& pe, uint32_t& rowbits, uint32_t& colbits)
+                                           double& pe, uint32_t& rowbits, uint32_t& colbits,
+                                           double* bstage = nullptr)
 {
     const size_t plane = (size_t)s.npad * s.npad;
     const int B = Y * kBlock + lane;
+    const bool staged = bstage != nullptr && X != Y;
+    double* my_stage = staged ? bstage + lane * kBStageRow : nullptr;
     for (int a = 0; a < a_end; ++a) {
         const bool valid = bvalid && (X != Y || lane < a);
         bool contact = false;
@@ -88,14 +106,41 @@ __device__ __forceinline__ void tile_pairs(const System& s, const ABlock& ab, in
             __stcs(pa, div_by_fixed<false>(fx, ma, rma));
             __stcs(pa + plane, div_by_fixed<false>(fy, ma, rma));
             __stcs(pa + 2 * plane, div_by_fixed<false>(fz, ma, rma));
-            double* pb = rowB + a;
-            __stcs(pb, div_by_fixed<false, true>(fx, mb, rmb));  // -(F/m[B]), sign set in the integer result
-            __stcs(pb + plane, div_by_fixed<false, true>(fy, mb, rmb));
-            __stcs(pb + 2 * plane, div_by_fixed<false, true>(fz, mb, rmb));
+            // -(F/m[B]), the sign set in the integer result
+            const double tbx = div_by_fixed<false, true>(fx, mb, rmb);
+            const double tby = div_by_fixed<false, true>(fy, mb, rmb);
+            const double tbz = div_by_fixed<false, true>(fz, mb, rmb);
+            if (staged) {
+                double* st = my_stage + (a & 3);
+                st[0] = tbx;
+                st[kBStagePlane] = tby;
+                st[2 * kBStagePlane] = tbz;
+            } else {
+                double* pb = rowB + a;
+                __stcs(pb, tbx);
+                __stcs(pb + plane, tby);
+                __stcs(pb + 2 * plane, tbz);
+            }
         }
         const uint32_t bal = __ballot_sync(0xffffffffu, contact);
         if (lane == a) rowbits = bal;
         if (contact) colbits |= 1u << a;
+        if (staged && bvalid && ((a & 3) == 3 || a == a_end - 1)) {
+            // row B, partners a0 .. a0+3: a 32-byte aligned sector (npad and
+            // 32X are multiples of 4, the buffer is 256-byte aligned)
+            const int a0 = a & ~3;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const double* st = my_stage + c * kBStagePlane;
+                const double v0 = st[0];
+                const double v1 = a0 + 1 < a_end ? st[1] : 0.0;
+                const double v2 = a0 + 2 < a_end ? st[2] : 0.0;
+                const double v3 = a0 + 3 < a_end ? st[3] : 0.0;
+                double2* dst = reinterpret_cast<double2*>(rowB + c * plane + a0);
+                __stcs(dst, make_double2(v0, v1));
+                __stcs(dst + 1, make_double2(v2, v3));
+            }
+        }
     }
 }
 
