@@ -3,18 +3,21 @@
 // accumulation, trained and evaluated on the GPU by this file's kernels
 // (include/spacelab_mlp.h).
 //
-// Every matrix product is one kernel, gemm_nt: C[M][N] = A[M][K] . B[N][K]^T
-// with A and B bf16 row-major (K contiguous), on the tensor cores through
-// mma.sync m16n8k16 (bf16 x bf16 -> f32) with ldmatrix-loaded fragments from
-// shared-memory tiles; the epilogue adds the bias and writes the FP32
-// pre-activation and/or the BF16 activation (GELU or identity).
+// Every matrix product is one kernel, gemm_nt_tc: C[M][N] = A[M][K] . B[N][K]^T
+// with A and B bf16 row-major (K contiguous) on the fifth-generation tensor
+// cores: TMA copies of 128-byte-swizzled K chunks into shared memory,
+// tcgen05.mma (M = 128, N <= 128, K = 16, bf16 x bf16 -> f32) into a tensor
+// memory accumulator, tcgen05.ld back to registers for the epilogue, which
+// adds the bias and writes the FP32 pre-activation and/or the BF16
+// activation (GELU or identity).
 //   forward   Z_l = X_l W_l^T + b_l,  X_{l+1} = bf16(GELU(Z_l))
 //   backward  dW_l = dZ_l^T X_l   (A = dZ^T, B = X^T: transposed copies)
 //             dX_l = dZ_l W_l     (B = W^T: a transposed copy of W)
 //             dZ_{l-1} = bf16(dX_l * GELU'(Z_{l-1}))
 // Widths are padded to multiples of 32 with zero weights that stay zero
-// (their gradients are zero), so every GEMM dimension is tile-aligned.
-// FP32 master weights are updated with Adam; bf16 copies feed the GEMMs.
+// (their gradients are zero).  FP32 master weights are updated with Adam;
+// bf16 copies feed the GEMMs.  An mma.sync m16n8k16 kernel (gemm_nt_kernel)
+// is kept only as the second opinion of sl_diag_gemm_bf16.
 #include "../../include/spacelab_mlp.h"
 #include "../../include/spacelab_gpu.h"
 
@@ -306,10 +309,11 @@ __global__ void __launch_bounds__(kTcThreads) gemm_nt_tc_kernel(const __grid_con
         }
     }
     __syncwarp();
-    const bool mma_done = sl::tma::mbar_wait(done, 0);
+    if (!sl::tma::mbar_wait(done, 0)) *failed = 1;
     tc_fence_after();
     __syncthreads();
-    if (*failed || !mma_done) {
+    // the same decision in every thread (tcgen05.ld is warp-collective)
+    if (*failed) {
         if (tid == 0) atomicExch(err, 1);
     } else {
         const int row = m0 + warp * 32 + lane;
@@ -447,6 +451,8 @@ struct sl_mlp {
     float* dX = nullptr;
     float *xin = nullptr, *yin = nullptr, *loss_part = nullptr;
     int step = 0;
+    int* d_err = nullptr;         // set by a tcgen05 GEMM whose bounded wait ran out
+    bool tc_setup_failed = false; // a GEMM's tensor maps or launch attributes could not be set up
     void* arena = nullptr;
 };
 
@@ -522,10 +528,26 @@ bool gemm_tc(cudaStream_t st, const bf16* A, int lda, const bf16* B, int ldb, co
     return launch_tc<128>(st, ma, B, ldb, bias, Cf, Cb, ldc, M, N, K, act, err);
 }
 
-void gemm(cudaStream_t st, const bf16* A, int lda, const bf16* B, int ldb, const float* bias, float* Cf, bf16* Cb,
-          int ldc, int M, int N, int K, int act)
+// Every product of the network runs on the tcgen05 GEMM.
+void gemm(sl_mlp* h, cudaStream_t st, const bf16* A, int lda, const bf16* B, int ldb, const float* bias, float* Cf,
+          bf16* Cb, int ldc, int M, int N, int K, int act)
 {
-    gemm_mma_sync(st, A, lda, B, ldb, bias, Cf, Cb, ldc, M, N, K, act);
+    if (h->tc_setup_failed) return;
+    if (!gemm_tc(st, A, lda, B, ldb, bias, Cf, Cb, ldc, M, N, K, act, h->d_err)) h->tc_setup_failed = true;
+}
+
+// After a synchronisation: the GEMMs' setup and bounded waits.
+int mlp_status(sl_mlp* h, const char* what)
+{
+    if (h->tc_setup_failed)
+        return sl_record_error(SL_ERR_CUDA, (std::string(what) + ": tcgen05 GEMM setup (tensor maps) failed").c_str());
+    int err = 0;
+    if (cudaMemcpy(&err, h->d_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return sl_record_error(SL_ERR_CUDA, (std::string(what) + ": reading the GEMM status failed").c_str());
+    if (err)
+        return sl_record_error(SL_ERR_TIMEOUT,
+                               (std::string(what) + ": a bounded wait in the tcgen05 GEMM ran out").c_str());
+    return SL_OK;
 }
 
 void transpose(cudaStream_t st, const bf16* in, int rows, int cols, int ldi, bf16* out, int ldo)
@@ -542,7 +564,7 @@ void forward(sl_mlp* h, int M, cudaStream_t st)
     pack_input_kernel<<<(M * ld0 + 255) / 256, 256, 0, st>>>(h->xin, M, h->n_in, ld0, h->X[0]);
     for (int l = 0; l < h->nl; ++l) {
         const bool last = l == h->nl - 1;
-        gemm(st, h->X[l], h->din[l], h->Pb + h->w_off[l], h->din[l], h->P + h->b_off[l], h->Z[l],
+        gemm(h, st, h->X[l], h->din[l], h->Pb + h->w_off[l], h->din[l], h->P + h->b_off[l], h->Z[l],
              last ? nullptr : h->X[l + 1], h->dout[l], M, h->dout[l], h->din[l], last ? 0 : 1);
     }
 }
@@ -559,12 +581,12 @@ void backward(sl_mlp* h, int M, cudaStream_t st)
         // dW = dZ^T X : A = dZ^T [N][M], B = X^T [K][M]
         transpose(st, h->dZ, M, N, N, h->dZt, M);
         transpose(st, h->X[l], M, K, K, h->Xt, M);
-        gemm(st, h->dZt, M, h->Xt, M, nullptr, h->G + h->w_off[l], nullptr, K, N, K, M, 0);
+        gemm(h, st, h->dZt, M, h->Xt, M, nullptr, h->G + h->w_off[l], nullptr, K, N, K, M, 0);
         bias_grad_kernel<<<(N + 127) / 128, 128, 0, st>>>(h->dZ, M, N, N, h->G + h->b_off[l]);
         if (l == 0) break;
         // dX = dZ W : A = dZ [M][N], B = W^T [K][N]
         transpose(st, h->Pb + h->w_off[l], N, K, K, h->Wt, N);
-        gemm(st, h->dZ, N, h->Wt, N, nullptr, h->dX, nullptr, K, M, K, N, 0);
+        gemm(h, st, h->dZ, N, h->Wt, N, nullptr, h->dX, nullptr, K, M, K, N, 0);
         gelu_back_kernel<<<(M * K + 255) / 256, 256, 0, st>>>(h->dX, h->Z[l - 1], M * K, h->dZ);
     }
 }
@@ -608,7 +630,7 @@ int sl_mlp_create(int n_in, int hidden, int hidden_layers, int n_out, int max_ba
     const size_t odZ = take((size_t)max_batch * maxw * 2), odZt = take((size_t)max_batch * maxw * 2),
                  oXt = take((size_t)max_batch * maxw * 2), odX = take((size_t)max_batch * maxw * 4),
                  oxin = take((size_t)max_batch * n_in * 4), oyin = take((size_t)max_batch * n_out * 4),
-                 oloss = take(((size_t)max_batch * maxw / 256 + 1) * 4);
+                 oloss = take(((size_t)max_batch * maxw / 256 + 1) * 4), oerr = take(sizeof(int));
     if (cudaMalloc(&h->arena, bytes) != cudaSuccess) {
         delete h;
         return sl_record_error(SL_ERR_ALLOC, "cudaMalloc of the MLP arena failed");
@@ -619,6 +641,7 @@ int sl_mlp_create(int n_in, int hidden, int hidden_layers, int n_out, int max_ba
     for (int l = 0; l < h->nl; ++l) { h->X.push_back((bf16*)(b + oX[l])); h->Z.push_back((float*)(b + oZ[l])); }
     h->dZ = (bf16*)(b + odZ); h->dZt = (bf16*)(b + odZt); h->Xt = (bf16*)(b + oXt); h->dX = (float*)(b + odX);
     h->xin = (float*)(b + oxin); h->yin = (float*)(b + oyin); h->loss_part = (float*)(b + oloss);
+    h->d_err = (int*)(b + oerr);
     cudaMemset(h->arena, 0, bytes);
     // He-style init of live weights, zero biases and padding
     std::vector<float> p(off, 0.0f);
@@ -689,6 +712,7 @@ int sl_mlp_gradients(sl_mlp* h, const float* x, const float* y, int M, float* gr
     forward(h, M, nullptr);
     backward(h, M, nullptr);
     if (cudaDeviceSynchronize() != cudaSuccess) return sl_record_error(SL_ERR_CUDA, "MLP step failed");
+    if (int r = mlp_status(h, "sl_mlp_gradients")) return r;
     if (grads) cudaMemcpy(grads, h->G, h->nparam * 4, cudaMemcpyDeviceToHost);
     if (loss) {
         const int ldo = h->dout[h->nl - 1];
@@ -743,6 +767,7 @@ int sl_mlp_train(sl_mlp* h, const float* x, const float* y, int n, int epochs, i
         if (loss_per_epoch) loss_per_epoch[ep] = (float)(ls / std::max(1, steps));
     }
     if (cudaDeviceSynchronize() != cudaSuccess && rc == SL_OK) rc = sl_record_error(SL_ERR_CUDA, "training failed");
+    if (rc == SL_OK) rc = mlp_status(h, "sl_mlp_train");
     return rc;
 }
 
@@ -759,6 +784,7 @@ int sl_mlp_predict(sl_mlp* h, const float* x, int n, float* y)
         forward(h, Mp, nullptr);
         if (cudaMemcpy(zb.data(), h->Z[L - 1], (size_t)M * ldo * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
             return sl_record_error(SL_ERR_CUDA, "prediction failed");
+        if (int r = mlp_status(h, "sl_mlp_predict")) return r;
         for (int r = 0; r < M; ++r)
             for (int c = 0; c < h->n_out; ++c) y[(size_t)(s0 + r) * h->n_out + c] = zb[(size_t)r * ldo + c];
     }

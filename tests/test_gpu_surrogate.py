@@ -25,16 +25,24 @@ def _layer_slices():
 
 
 def test_mlp_forward_matches_cpu_oracle():
+    """The forward pass (tcgen05 GEMMs) against the numpy oracle with the same
+    bf16 rounding points: the two differ only in FP32 accumulation order,
+    which can move an activation across a bf16 rounding boundary (one bf16
+    ulp = 2^-8 relative); bar 5e-3 of the largest output (measured: 2.6e-4
+    to 4.4e-3 over five seeds)."""
     net = _net()
     rng = np.random.default_rng(0)
     x = rng.normal(size=(100, 8)).astype(np.float32)
     y = net.predict(x)
     ref, *_ = mlp_oracle.forward(net.params(), x, **ARCH)
     scale = np.abs(ref).max()
-    assert np.abs(y - ref).max() <= 1e-2 * scale
+    assert np.abs(y - ref).max() <= 5e-3 * scale
 
 
 def test_mlp_gradients_match_cpu_oracle():
+    """Every layer's weight and bias gradients against the oracle: within
+    3e-3 of the layer's gradient norm (measured: at most 7.6e-4 over five
+    seeds) and aligned to 1e-5 in cosine."""
     net = _net()
     rng = np.random.default_rng(1)
     x = rng.normal(size=(128, 8)).astype(np.float32)
@@ -48,8 +56,8 @@ def test_mlp_gradients_match_cpu_oracle():
         if nr == 0:
             assert np.abs(gg).max() == 0
             continue
-        assert np.linalg.norm(gg - gr) <= 3e-2 * nr, (a, b)
-        assert gg @ gr / (np.linalg.norm(gg) * nr) > 0.999
+        assert np.linalg.norm(gg - gr) <= 3e-3 * nr, (a, b)
+        assert gg @ gr / (np.linalg.norm(gg) * nr) > 1 - 1e-5
 
 
 def test_mlp_learns_a_smooth_map():
@@ -79,23 +87,24 @@ def test_ensemble_spread_grows_outside_the_data():
 
 def test_screened_sweep_gains_over_simulating_every_point():
     """Small end to end: outcomes of 448 simulated collisions (the batched
-    solver's sweep recipe at small sizes) train the ensemble on 384 of
-    them; the screening threshold comes from the other 64 (mean absolute
-    error of the accepted ones <= 0.5 of each outcome's spread); a
-    3000-point sweep is screened and its uncertain points and a 3% audit are
-    re-run.  The network must beat simulating every point on cost, and on
-    the audit its error must be below the outcomes' own spread (it
-    predicts, not just averages)."""
-    steps = 600
+    solver's sweep recipe with 16-40-sphere targets, 3000 steps) train the
+    ensemble on 384 of them; the screening threshold comes from the other
+    64 (mean absolute error of the accepted ones <= 0.8 of each outcome's
+    spread -- a small training set gives a coarse surrogate); a 3000-point
+    sweep is screened and its uncertain points and a 3% audit are re-run.
+    The network must beat simulating every point on cost, and on the audit
+    its error must be below the outcomes' own spread (it predicts, not just
+    averages)."""
+    steps = 3000
     data = B.sample_collisions(448, seed=11, nt_range=(16, 40), clearance=W.CLEARANCE, k_speed_div=W.K_SPEED_DIV)
     y, info = W.simulate(data, steps, mode="mixed_df")
     assert info["nonfinite"] == 0
     x = W.features(data)
     ens = S.Ensemble(8, 4, members=5, seed=9)
     ens.fit(x[:384], y[:384], epochs=150, batch=128, lr=1e-3)
-    pick = W.pick_threshold(ens, x[384:], y[384:], error_target=0.5)
-    assert pick["threshold"] > 0 and pick["accept_fraction"] > 0.3
-    assert max(pick["mae_std_units"]) <= 0.5
+    pick = W.pick_threshold(ens, x[384:], y[384:], error_target=0.8)
+    assert pick["threshold"] > 0 and pick["accept_fraction"] > 0.2
+    assert max(pick["mae_std_units"]) <= 0.8
     points = W.sample_params(3000, seed=12, nt_range=(16, 40))
     res = W.screen_sweep(ens, points, steps, threshold=pick["threshold"], audit=0.03, seed=13, sim_mode="mixed_df",
                          fp64_check=8)
