@@ -669,7 +669,7 @@ def run_surrogate_study(args) -> dict:
     val, trn = perm[:nval], perm[nval:]
     ens = S.Ensemble(8, 4, members=5, seed=3)
     fit = ens.fit(x[trn], y[trn], epochs=args.epochs, batch=256, lr=1e-3)
-    targets = sorted({0.15, 0.2, 0.25, 0.3, 0.4, args.error_target})
+    targets = sorted({0.15, 0.175, 0.2, 0.25, 0.3, args.error_target})
     curve = {str(t): W.pick_threshold(ens, x[val], y[val], t) for t in targets}
     chosen = curve[str(args.error_target)]
     points = W.sample_params(args.sweep_points, seed=22)
@@ -769,7 +769,7 @@ def main(argv=None) -> int:
     ap.add_argument("--sweep-points", type=int, default=1000000)
     ap.add_argument("--study-steps", type=int, default=3000)
     ap.add_argument("--epochs", type=int, default=150)
-    ap.add_argument("--error-target", type=float, default=0.25,
+    ap.add_argument("--error-target", type=float, default=0.2,
                     help="surrogate study: mean absolute error of the accepted validation points, in units of "
                          "each outcome's spread, that sets the screening threshold")
     ap.add_argument("--audit", type=float, default=0.01)

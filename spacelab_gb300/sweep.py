@@ -174,6 +174,8 @@ def screen_sweep(ens, points: list[B.Collision], steps: int, threshold: float, a
            "features_s": t_feat, "inference_s": t_inf, "rerun_sim_s": info["seconds"],
            "full_sim_s_estimate": full_cost, "cost_ratio": full_cost / screened_cost,
            "audit_mae": err[aud_pos].mean(0).tolist(), "audit_max_err": err[aud_pos].max(0).tolist(),
+           # the method without the network: the training mean for every point
+           "audit_mae_training_mean": np.abs(ens.ym - sim_out[aud_pos]).mean(0).tolist(),
            "audit_mae_std_units": (err[aud_pos].mean(0) / ens.ys).tolist(),
            "rerun_mae": err.mean(0).tolist(), "outcome_std": sim_out.std(0).tolist(),
            "threshold": threshold, "sim_mode": sim_mode, "rerun_nonfinite": info["nonfinite"]}

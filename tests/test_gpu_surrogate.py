@@ -86,23 +86,23 @@ def test_ensemble_spread_grows_outside_the_data():
 
 
 def test_screened_sweep_gains_over_simulating_every_point():
-    """Small end to end: outcomes of 448 simulated collisions (the batched
+    """Small end to end: outcomes of 1280 simulated collisions (the batched
     solver's sweep recipe with 16-40-sphere targets, 3000 steps) train the
-    ensemble on 384 of them; the screening threshold comes from the other
-    64 (mean absolute error of the accepted ones <= 0.8 of each outcome's
+    ensemble on 1024 of them; the screening threshold comes from the other
+    256 (mean absolute error of the accepted ones <= 0.8 of each outcome's
     spread -- a small training set gives a coarse surrogate); a 3000-point
     sweep is screened and its uncertain points and a 3% audit are re-run.
     The network must beat simulating every point on cost, and on the audit
-    its error must be below the outcomes' own spread (it predicts, not just
-    averages)."""
+    it must beat the method without it -- predicting the training mean --
+    on every outcome that varies."""
     steps = 3000
-    data = B.sample_collisions(448, seed=11, nt_range=(16, 40), clearance=W.CLEARANCE, k_speed_div=W.K_SPEED_DIV)
+    data = B.sample_collisions(1280, seed=11, nt_range=(16, 40), clearance=W.CLEARANCE, k_speed_div=W.K_SPEED_DIV)
     y, info = W.simulate(data, steps, mode="mixed_df")
     assert info["nonfinite"] == 0
     x = W.features(data)
     ens = S.Ensemble(8, 4, members=5, seed=9)
-    ens.fit(x[:384], y[:384], epochs=150, batch=128, lr=1e-3)
-    pick = W.pick_threshold(ens, x[384:], y[384:], error_target=0.8)
+    ens.fit(x[:1024], y[:1024], epochs=150, batch=128, lr=1e-3)
+    pick = W.pick_threshold(ens, x[1024:], y[1024:], error_target=0.8)
     assert pick["threshold"] > 0 and pick["accept_fraction"] > 0.2
     assert max(pick["mae_std_units"]) <= 0.8
     points = W.sample_params(3000, seed=12, nt_range=(16, 40))
@@ -113,7 +113,9 @@ def test_screened_sweep_gains_over_simulating_every_point():
     mae = np.array(res["audit_mae"])
     spread = np.array(res["outcome_std"])
     informative = spread > 1e-9
-    assert np.all(mae[informative] < spread[informative])
+    # the method without the network, on the same audit points
+    mean_only = np.array(res["audit_mae_training_mean"])
+    assert np.all(mae[informative] < mean_only[informative]), (mae, mean_only)
     # the mixed re-runs stand for the FP64 method: their outcomes agree to a
     # small part of each outcome's spread
     d = np.array(res["fp64_check"]["mean_abs_diff"])
