@@ -261,7 +261,7 @@ int sl_create(int n, const sl_material* mat, int mode, sl_handle** out)
     const size_t o_red = take(sl::kRedBlocks * 8 * sizeof(double));
     const size_t o_en = take(8 * sizeof(double));
     const size_t o_st = take(sizeof(unsigned int));
-    const size_t o_tc = take(mixed ? sizeof(int) : 0);
+    const size_t o_tc = take(sl::kPairPhases * sizeof(int));  // the pair kernels' work queues
     const size_t o_cf = take(mixed ? np * sizeof(int) : 0);
     const size_t o_scl = take(sizeof(sl::Scalars));
     const size_t o_dstage = take(6 * 3 * np * sizeof(double));
@@ -296,10 +296,8 @@ int sl_create(int n, const sl_material* mat, int mode, sl_handle** out)
     s.red = reinterpret_cast<double*>(base + o_red);
     s.energy = reinterpret_cast<double*>(base + o_en);
     s.status = reinterpret_cast<unsigned int*>(base + o_st);
-    if (mixed) {
-        s.tile_counter = reinterpret_cast<int*>(base + o_tc);
-        s.contact_flag = reinterpret_cast<int*>(base + o_cf);
-    }
+    s.tile_counter = reinterpret_cast<int*>(base + o_tc);
+    if (mixed) s.contact_flag = reinterpret_cast<int*>(base + o_cf);
     h->d_sc = reinterpret_cast<sl::Scalars*>(base + o_scl);
     h->d_stage = reinterpret_cast<double*>(base + o_dstage);
     s.sc = h->d_sc;

@@ -77,8 +77,9 @@ struct System {
     // (FP64): entry (c, K, i) is component c of the force on sphere i from
     // the partners in 32-sphere block K
     double* part64;
-    // mixed form: the pair kernel's tile counter, and per sphere a flag set
-    // when any of its pairs is in contact (both zeroed by the drift kernel)
+    // the pair kernels' tile counters, one per pair phase (NULL: static
+    // tile stride), and, mixed forms, per sphere a flag set when any of its
+    // pairs is in contact (both zeroed by the drift kernel)
     int* tile_counter;
     int* contact_flag;
     int len_shift;

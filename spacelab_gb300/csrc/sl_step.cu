@@ -45,7 +45,8 @@ __global__ void __launch_bounds__(kDriftThreads) drift_kernel(const __grid_const
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 3 * s.n) return;
-    if (t == 0 && s.tile_counter) *s.tile_counter = 0;  // the mixed pair kernel's work queue
+    if (t == 0 && s.tile_counter)  // the pair kernels' work queues
+        for (int k = 0; k < kPairPhases; ++k) s.tile_counter[k] = 0;
     if (t < s.n && s.contact_flag) s.contact_flag[t] = 0;
     const int c = t / s.n;
     const int i = t - c * s.n;
@@ -86,7 +87,8 @@ __device__ __forceinline__ void col_tile_coords(int nb, long long u, int& X, int
 }
 
 template <bool WRITE>
-__global__ void __launch_bounds__(128, 4) pair_tile_kernel(const __grid_constant__ System s, int c0, int c1)
+__global__ void __launch_bounds__(128, 4) pair_tile_kernel(const __grid_constant__ System s, int c0, int c1,
+                                                          int phase)
 {
     __shared__ ABlock sA[4];
     __shared__ double sB[4][kBStageDoubles];
@@ -97,8 +99,13 @@ __global__ void __launch_bounds__(128, 4) pair_tile_kernel(const __grid_constant
     const double Ha = s.mat.Ha;
     const long long h_min_bits = __double_as_longlong(s.mat.h_min);  // h_min > 0
 
-    const long long u1 = col_offset(s.nb, c1);
-    for (long long u = col_offset(s.nb, c0) + (long long)blockIdx.x * 4 + wib; u < u1; u += nwarps) {
+    // A first round of tiles in warp order; then whichever warp is free takes
+    // the next tile from the launch's counter (zeroed by the drift kernel),
+    // or, without a counter, the static stride.  A tile's results do not
+    // depend on the warp that computes it.
+    const long long u0 = col_offset(s.nb, c0), u1 = col_offset(s.nb, c1);
+    int* counter = s.tile_counter ? s.tile_counter + phase : nullptr;
+    for (long long u = u0 + (long long)blockIdx.x * 4 + wib; u < u1;) {
         int X, Y;
         col_tile_coords(s.nb, u, X, Y);
         const long long t = (long long)X * (X + 1) / 2 + Y;  // this tile's PE slot
@@ -144,6 +151,13 @@ __global__ void __launch_bounds__(128, 4) pair_tile_kernel(const __grid_constant
             if (lane == 0) s.pe_tile[t] = pe;
         }
         __syncwarp();
+        if (counter) {
+            int next = 0;
+            if (lane == 0) next = atomicAdd(counter, 1);
+            u = u0 + nwarps + __shfl_sync(0xffffffffu, next, 0);
+        } else {
+            u += nwarps;
+        }
     }
 }
 
@@ -403,15 +417,15 @@ static void launch_rowsum(const System& s, cudaStream_t st, const CUtensorMap* m
         rowsum_kernel<<<(3 * s.n + kRowThreads - 1) / kRowThreads, kRowThreads, 0, st>>>(s, b0, b1, first, last);
 }
 
-static void launch_pair_columns(const System& s, bool write, int num_sms, cudaStream_t st, int c0, int c1)
+static void launch_pair_columns(const System& s, bool write, int num_sms, cudaStream_t st, int c0, int c1, int phase)
 {
     const long long tiles = ((long long)c1 * s.nb - (long long)c1 * (c1 - 1) / 2) -
                             ((long long)c0 * s.nb - (long long)c0 * (c0 - 1) / 2);
     const int pb = pair_grid_blocks(tiles, num_sms);
     if (write)
-        pair_tile_kernel<true><<<pb, 128, 0, st>>>(s, c0, c1);
+        pair_tile_kernel<true><<<pb, 128, 0, st>>>(s, c0, c1, phase);
     else
-        pair_tile_kernel<false><<<pb, 128, 0, st>>>(s, c0, c1);
+        pair_tile_kernel<false><<<pb, 128, 0, st>>>(s, c0, c1, phase);
 }
 
 void launch_step(const System& s, bool write, int num_sms, cudaStream_t st, StepTimers* tm, const StepOverlap* ov,
@@ -422,12 +436,12 @@ void launch_step(const System& s, bool write, int num_sms, cudaStream_t st, Step
     int cb[kPairPhases + 1];
     const int np = ov ? phase_bounds(s.nb, cb) : 1;
     if (np <= 1) {
-        launch_pair_columns(s, write, num_sms, st, 0, s.nb);
+        launch_pair_columns(s, write, num_sms, st, 0, s.nb, 0);
         if (tm) cudaEventRecord(tm->ev[1], st);
         launch_rowsum(s, st, map, 0, s.nb, 1, 1, num_sms);
     } else {
         for (int p = 0; p < np; ++p) {
-            launch_pair_columns(s, write, num_sms, st, cb[p], cb[p + 1]);
+            launch_pair_columns(s, write, num_sms, st, cb[p], cb[p + 1], p);
             cudaEventRecord(ov->phase[p], st);
             cudaStreamWaitEvent(ov->side, ov->phase[p], 0);
             launch_rowsum(s, ov->side, map, cb[p], cb[p + 1], p == 0, p == np - 1, num_sms);
