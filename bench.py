@@ -459,6 +459,27 @@ def run_ours(args, rank, world, local_rank) -> dict | None:
     achieved = work / (pair_ms_avg * 1e-3) / 1e12
     traffic = _read_profile_traffic() if (args.mode == "exact" and w.name == "aggregate_collision_n5000") else None
 
+    # the schedule's write steps (every w.skip steps; none may fall in a short
+    # timed window): one write step timed alone, on the library's stream, and
+    # the per-step average of the schedule (skip - 1 plain steps, one write)
+    wev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    write_ms = []
+    for _ in range(3):
+        wev[0].record(stream)
+        sim.step(1, write_last=True)
+        wev[1].record(stream)
+        torch.cuda.synchronize()
+        write_ms.append(wev[0].elapsed_time(wev[1]))
+    next_step += 3
+    write_step_ms = float(np.median(write_ms))
+    plain_ms = ms_max / args.steps if nwrites == 0 else None
+    schedule = None
+    if plain_ms is not None:
+        sched_ms = ((w.skip - 1) * plain_ms + write_step_ms) / w.skip
+        schedule = {"write_step_ms": write_step_ms, "plain_step_ms": plain_ms, "ms_per_step": sched_ms,
+                    "value": w.pairs_per_step * world / (sched_ms * 1e-3),
+                    "how": f"one write step every {w.skip} steps: ({w.skip - 1} x plain + 1 x write) / {w.skip}"}
+
     # end to end through the C ABI with host buffers (upload + step + download)
     e2e = run_e2e(sim, w, min(args.steps, 60), first_step=next_step)
     pair_kernel = sim.pair_kernel()
@@ -480,6 +501,7 @@ def run_ours(args, rank, world, local_rank) -> dict | None:
                                "contacts_after_timed_steps": contacts_end}, mode=args.mode),
         "impl": "ours",
         "e2e": e2e,
+        "schedule_average": schedule,
         "gpu_launches": gpu_launches,
         "roofline": {"bound": bound,
                      "kernel": pair_kernel,
