@@ -543,26 +543,28 @@ def run_e2e(sim, w, steps: int, first_step: int = 1) -> dict:
     lib = _lib.lib()
     n = w.n
     pin = lambda: torch.zeros(3 * n, dtype=torch.float64).pin_memory().numpy()  # noqa: E731
-    pos, vel, wv, acc, aacc, prev = (pin() for _ in range(6))
+    pos, vel, wv, acc, aacc = (pin() for _ in range(5))
     sim.download()
     pos[:] = sim.group.pos.reshape(-1); vel[:] = sim.group.vel.reshape(-1); wv[:] = sim.group.w.reshape(-1)
-    acc[:] = sim.group.acc.reshape(-1); aacc[:] = sim.group.aacc.reshape(-1); prev[:] = pos
+    acc[:] = sim.group.acc.reshape(-1); aacc[:] = sim.group.aacc.reshape(-1)
     h = sim.handle
     # the host buffers stay put: their pointers are formed once, as a C
-    # caller would hold them
+    # caller would hold them.  The state is the end of a step, so the
+    # previous-step positions that choose kin/kout are the uploaded ones
+    # (pos_prev NULL), as the reference's `distances` hold the pair distances
+    # of the current positions between steps.
     P = _lib.dptr
-    pp, pv, pw, pa, paa, ppr = P(pos), P(vel), P(wv), P(acc), P(aacc), P(prev)
+    pp, pv, pw, pa, paa = P(pos), P(vel), P(wv), P(acc), P(aacc)
     e = _lib.Energy()
     pe = ctypes.byref(e)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for k in range(steps):
-        _lib.check(lib.sl_upload_resume(h, pp, pv, pw, pa, paa, ppr), "sl_upload_resume")
-        prev[:] = pos
+        _lib.check(lib.sl_upload_resume(h, pp, pv, pw, pa, paa, None), "sl_upload_resume")
         _lib.check(lib.sl_step(h, 1, int((first_step + k) % w.skip == 0), pe), "sl_step")
         _lib.check(lib.sl_download(h, pp, pv, pw, pa, paa), "sl_download")
     el = time.perf_counter() - t0
-    return {"value": w.pairs_per_step * steps / el, "unit": UNIT, "h2d_bytes_per_step": 6 * 3 * n * 8,
+    return {"value": w.pairs_per_step * steps / el, "unit": UNIT, "h2d_bytes_per_step": 5 * 3 * n * 8,
             "d2h_bytes_per_step": 5 * 3 * n * 8, "steps": steps, "first_step": first_step,
             "api": "sl_upload_resume + sl_step(1) + sl_download per step"}
 

@@ -500,13 +500,11 @@ template <int BN>
 bool launch_tc(cudaStream_t st, const CUtensorMap& ma, const bf16* B, int ldb, const float* bias, float* Cf, bf16* Cb,
                int ldc, int M, int N, int K, int act, int* err)
 {
-    static bool attr_set = false;  // per BN; the attribute is per function
-    if (!attr_set) {
-        if (cudaFuncSetAttribute(gemm_nt_tc_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 TcSmem<BN>::kBytes) != cudaSuccess)
-            return false;
-        attr_set = true;
-    }
+    // set on every call: the attribute belongs to the current device's
+    // context, and the call is a host-side table update
+    if (cudaFuncSetAttribute(gemm_nt_tc_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcSmem<BN>::kBytes) !=
+        cudaSuccess)
+        return false;
     CUtensorMap mb;
     if (!make_tc_map(&mb, B, N, K, ldb, BN)) return false;
     dim3 grid((N + BN - 1) / BN, (M + kTcM - 1) / kTcM);
