@@ -88,3 +88,34 @@ def test_aggregate_collision_n5000_5000_steps_through_impact():
     # the impact is inside the compared window
     assert seen[100] == 0
     assert max(seen.values()) > 0, seen
+
+
+def test_polydisperse_cluster_n20000_exact_matches_oracle():
+    """The 20000-sphere polydisperse workload (lognormal radii, so every tile
+    takes the general, unequal-radius form) in the exact mode: 30 steps with
+    a write step every 10, bit-identical to the oracle at steps 10 and 30,
+    the contact set identical, energy rows to the usual bars.  (The workload's
+    10,000 steps are the mixed forms' drift runs, bench.py --drift-steps.)"""
+    w = configs.polydisperse_cluster_20000()
+    assert w.n == 20000
+    g = w.group
+    sim = GpuStep(g.copy(), w.material, "exact")
+    sim.set_scalars(w.dt, w.kin, w.kout)
+    o = CpuOracle(g.pos, g.vel, g.w, g.R, g.m, g.moi, w.material, w.dt, w.kin, w.kout)
+    try:
+        _assert_energy(sim.init_conditions(), o.init(), o.state(), g.m, g.moi)
+        assert np.array_equal(sim.contacts(), o.contacts())
+        for step in range(1, 31):
+            write = step % 10 == 0
+            e = sim.sim_one_step(write)
+            eo = o.step(write, threads=0)
+            if write:
+                _assert_energy(e, eo, o.state(), g.m, g.moi)
+            if step in (10, 30):
+                st, so = _state(sim), o.state()
+                for key in STATE_KEYS:
+                    assert np.array_equal(st[key], so[key]), (step, key)
+                assert np.array_equal(sim.contacts(), o.contacts())
+    finally:
+        sim.close()
+        o.close()
