@@ -25,6 +25,7 @@
 #include "sl_fp64_exact.cuh"
 #include "sl_pair_exact.cuh"
 #include "sl_tile_exact.cuh"
+#include "sl_vdw_energy.cuh"
 
 namespace sl {
 
@@ -109,7 +110,7 @@ __device__ double pair_pass(const Batch& b, int off, int n, const Material& M, d
                         fx = coef * div_by_rsqrt(rx, dist, Y, p);
                         fy = coef * div_by_rsqrt(ry, dist, Y, p);
                         fz = coef * div_by_rsqrt(rz, dist, Y, p);
-                        if (WRITE && iA) pe += vdw_energy(M.Ha, h, RA, RB, twoRA);
+                        if (WRITE && iA) pe += vdw_energy_far_df(M.Ha, h, RA, RB, twoRA);
                     }
                     const double qx = div_by_fixed<false>(fx, mi, rmi);              // :249-250
                     const double qy = div_by_fixed<false>(fy, mi, rmi);

@@ -7,6 +7,7 @@
 #include "sl_device.cuh"
 #include "sl_fp64_exact.cuh"
 #include "sl_pair_exact.cuh"
+#include "sl_vdw_energy.cuh"
 
 namespace sl {
 
@@ -97,7 +98,7 @@ __device__ __forceinline__ void tile_pairs(const System& s, const ABlock& ab, in
                 fx = coef * div_by_rsqrt(rx, dist, Yr, p);                    // :221-227
                 fy = coef * div_by_rsqrt(ry, dist, Yr, p);
                 fz = coef * div_by_rsqrt(rz, dist, Yr, p);
-                if (WRITE) pe += vdw_energy(Ha, h, Ra, Rb, ab.twoR[a]);                    // :239
+                if (WRITE) pe += vdw_energy_far_df(Ha, h, Ra, Rb, ab.twoR[a]);             // :239
             }
             // :249-250 -- acc[A] += F/m[A]; acc[B] -= F/m[B] (stored negated)
             const double ma = ab.m[a];
