@@ -379,6 +379,8 @@ def run_ours(args, rank, world, local_rank) -> dict | None:
     sim = GpuStep(g.copy(), w.material, args.mode)
     if args.overlap:
         sim.set_overlap(True)
+    if args.mode == "exact":
+        sim.set_rowsum(args.rowsum)
     sim.set_scalars(w.dt, w.kin, w.kout)
     sim.init_conditions()
     stream = torch.cuda.ExternalStream(sim.stream_ptr())
@@ -529,6 +531,7 @@ def run_ours(args, rank, world, local_rank) -> dict | None:
         "data": "synthetic (seeded clusters; no dataset)",
         "config": _config(w, {"parallelism": "replicas" if world > 1 else "single GPU", "mode": args.mode,
                                "overlap": bool(args.overlap), "start_step": start,
+                               **({"rowsum": args.rowsum} if args.mode == "exact" else {}),
                                "timed_steps": [first, first + args.steps - 1], "write_steps_timed": nwrites,
                                "contacts_at_start_step": contacts_start,
                                "contacts_after_timed_steps": contacts_end}, mode=args.mode),
@@ -812,6 +815,9 @@ def main(argv=None) -> int:
                          "(--batched runs exact or mixed_df)")
     ap.add_argument("--overlap", action="store_true",
                     help="exact mode: run the row sums beside the pair phases (sl_set_overlap)")
+    ap.add_argument("--rowsum", choices=["int", "fp64"], default="fp64",
+                    help="exact mode: the row sums' FP64 additions on the FP64 unit (default) or the integer pipe "
+                         "(sl_set_rowsum); identical results")
     ap.add_argument("--workload", choices=WORKLOADS, default="aggregate_collision_n5000")
     ap.add_argument("--drift-steps", type=int, default=0,
                     help="instead of the benchmark: run the mixed and the FP64 form side by side for this many "

@@ -168,6 +168,16 @@ void* sl_stream(sl_handle* h);
  * mixed modes have no pipelined form (SL_ERR_UNSUPPORTED for enable != 0). */
 int sl_set_overlap(sl_handle* h, int enable);
 
+/* How exact mode adds each sphere's pair terms in the reference's order
+ * (ColliderSingleCore.cpp:249-250).  SL_ROWSUM_FP64 (the default) uses
+ * the FP64 unit; SL_ROWSUM_INT computes every FP64 addition, correctly
+ * rounded, on the integer pipe.  The sums are identical bit for bit either
+ * way; only the time differs.  Exact mode only (SL_ERR_UNSUPPORTED for the
+ * mixed modes, which keep no per-pair terms). */
+#define SL_ROWSUM_INT 0
+#define SL_ROWSUM_FP64 1
+int sl_set_rowsum(sl_handle* h, int method);
+
 /* Kernel launches one step makes (a write step computes the energy too). */
 int sl_step_launches(const sl_handle* h, int write, int* count);
 

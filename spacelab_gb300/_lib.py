@@ -72,6 +72,7 @@ _PROTOS = [
     ("sl_contacts", ctypes.c_int, [ctypes.c_void_p, _c_int_p, ctypes.c_long, ctypes.POINTER(ctypes.c_long)]),
     ("sl_stream", ctypes.c_void_p, [ctypes.c_void_p]),
     ("sl_set_overlap", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    ("sl_set_rowsum", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     ("sl_step_launches", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
     ("sl_pair_kernel", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_char_p)]),
     ("sl_kernel_timing", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),

@@ -224,6 +224,12 @@ class GpuStep:
         """Exact mode: pipeline the row sums with the pair phases (default off)."""
         check(self._lib.sl_set_overlap(self._h, int(enable)), "sl_set_overlap")
 
+    def set_rowsum(self, method: str) -> None:
+        """Exact mode: "fp64" (default) adds each row's FP64 terms on the FP64
+        unit, "int" exactly on the integer pipe; the sums are identical."""
+        code = {"int": 0, "fp64": 1}[method]
+        check(self._lib.sl_set_rowsum(self._h, code), "sl_set_rowsum")
+
     def step_launches(self, write: bool) -> int:
         """Kernel launches of one step."""
         c = ctypes.c_int()

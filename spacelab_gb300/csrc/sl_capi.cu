@@ -67,6 +67,7 @@ struct sl_handle {
     bool has_map = false;     // the TMA row sums are ready (exact form)
     bool has_ov = false;   // ov's stream and events exist
     bool overlap = false;  // steps use them
+    bool rowsum_int = false;  // exact row sums: FP64 additions on the integer pipe (else the FP64 unit)
     void* arena = nullptr;
     size_t arena_bytes = 0;
     double* staging = nullptr;  // pinned, 18 * npad doubles (per-sphere scalars at upload)
@@ -105,7 +106,7 @@ void launch_mode_step(sl_handle* h, bool write, sl::StepTimers* tm)
         sl::launch_step_mixed(h->sys, write, h->num_sms, h->stream, tm);
     else
         sl::launch_step(h->sys, write, h->num_sms, h->stream, tm, h->overlap ? &h->ov : nullptr,
-                        h->has_map ? &h->pair_map : nullptr);
+                        h->has_map ? &h->pair_map : nullptr, h->rowsum_int);
 }
 
 // One step on the handle's stream, with optional timing events.
@@ -572,6 +573,18 @@ int sl_set_overlap(sl_handle* h, int enable)
     SL_CUDA(cudaStreamSynchronize(h->stream));
     if (h->overlap != (enable != 0)) drop_graph(h);
     h->overlap = enable != 0;
+    return SL_OK;
+}
+
+int sl_set_rowsum(sl_handle* h, int method)
+{
+    if (int r = check_handle(h)) return r;
+    if (method != SL_ROWSUM_INT && method != SL_ROWSUM_FP64) return fail(SL_ERR_ARG, "unknown row-sum method");
+    if (h->mode != SL_MODE_EXACT) return fail(SL_ERR_UNSUPPORTED, "the row-sum method applies to exact mode only");
+    SL_CUDA(cudaStreamSynchronize(h->stream));
+    const bool want = method == SL_ROWSUM_INT;
+    if (h->rowsum_int != want) drop_graph(h);
+    h->rowsum_int = want;
     return SL_OK;
 }
 

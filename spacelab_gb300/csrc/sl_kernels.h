@@ -37,16 +37,18 @@ void launch_stage_out(const System& s, double* const dst[6], Vec3Soa* const arr[
 // map: a tensor map of the pair-term buffer (make_pair_map) selects the
 // TMA-streamed row sums; NULL the plain-load form.
 void launch_step(const System& s, bool write, int num_sms, cudaStream_t st, StepTimers* tm,
-                 const StepOverlap* ov = nullptr, const CUtensorMap* map = nullptr);
+                 const StepOverlap* ov = nullptr, const CUtensorMap* map = nullptr, bool int_adds = true);
 // Prepares the TMA row sums of the exact form: the tensor map of the
 // pair-term buffer (FP64) and the kernels' shared-memory limits; false if
 // that fails (the plain-load row sums are used then).
 bool make_pair_map(const System& s, CUtensorMap* map);
 // The TMA-streamed ordered row sums over partner blocks [b0, b1) with terms
-// of type T (double); first/last as for the plain row sums.
+// of type T (double); first/last as for the plain row sums.  int_adds: each
+// FP64 addition on the integer pipe (rowsum_int_kernel), else on the FP64
+// unit (rowsum_tma_kernel); the sums are identical.
 template <typename T>
 void launch_rowsum_tma(const System& s, const CUtensorMap& map, int b0, int b1, int first, int last, int num_sms,
-                       cudaStream_t st);
+                       bool int_adds, cudaStream_t st);
 // Status bit set by a kernel whose bounded wait for a TMA copy ran out.
 constexpr unsigned kStatusWaitTimeoutBit = 2u;
 // The double-float mixed form (SL_MODE_MIXED_DF, sl_step_mixed.cu).

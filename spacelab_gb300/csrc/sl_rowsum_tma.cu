@@ -33,6 +33,7 @@
 // unit bounds.
 #include "sl_device.cuh"
 #include "sl_kernels.h"
+#include "sl_sum_exact.cuh"
 #include "sl_tma.cuh"
 
 #include <cudaTypedefs.h>
@@ -80,11 +81,13 @@ struct RsTerm<double> {
     };
 };
 
-template <typename T, int BPS>
+// Issues stage q (BPS boxes) into buffer q % NST of the warp's NST stage
+// buffers, completing barrier full[q % NST].
+template <typename T, int BPS, int NST = kRsStages>
 __device__ __forceinline__ void rs_issue(unsigned char* buf, uint64_t* full, const CUtensorMap* map, int q, int x0,
                                          int row0)
 {
-    const int st = q % kRsStages;
+    const int st = q % NST;
     unsigned char* dst = buf + st * RsStage<BPS>::kBytes;
     tma::mbar_arrive_expect_tx(&full[st], RsStage<BPS>::kBytes);
 #pragma unroll
@@ -219,6 +222,158 @@ __global__ void __launch_bounds__(32 * kRsWarps, 8 / BPS) rowsum_tma_kernel(cons
     if (!isfinite(v) || !isfinite(wv) || !isfinite(s.pos.c[c][i])) atomicOr(s.status, 1u);
 }
 
+// ---------------------------------------------------------------------------
+// rowsum_int_kernel: the same ordered sums with each FP64 addition computed
+// on the integer pipe (sl_sum_exact.cuh) instead of the FP64 unit
+// (SL_ROWSUM_INT).  On GB300 it is the slower of the two at N=5000 (0.38
+// against 0.23 ms): ~49 ALU instructions per addition at the ALU pipe's
+// half rate outweigh the FP64 unit's 64-76-cycle dependent adds.
+//
+// Same mapping as rowsum_tma_kernel (one warp per (component, 32-row block),
+// lane = row, rows streamed in 16-column TMA boxes), and a box is one chunk
+// of 16 additions: the running sum at the chunk's start is kept, the 16
+// additions run in the frame form, and a lane whose fast path left its
+// domain (a binade prediction that failed, a jump of more than 8 binades, a
+// term larger than the new sum) repeats the chunk with FP64 additions.  Both
+// paths give RN(s + t) at every addition, in the reference's order, so the
+// sums are the FP64 kernel's bit for bit.  Padding rows (i >= n, all terms
+// +0.0, never stored) take no part in the warp's vote, so their zero sums
+// cost no repeats.
+constexpr int kIsStages = 4;                            // boxes in flight per warp
+constexpr int kIsSmem = kRsWarps * kIsStages * kRsBox + 1024;
+
+__device__ __forceinline__ uint64_t is_lo(const uint4& u) { return ((uint64_t)u.y << 32) | u.x; }
+__device__ __forceinline__ uint64_t is_hi(const uint4& u) { return ((uint64_t)u.w << 32) | u.z; }
+
+__global__ void __launch_bounds__(32 * kRsWarps, 8) rowsum_int_kernel(const __grid_constant__ System s,
+                                                                       const __grid_constant__ CUtensorMap map,
+                                                                       int b0, int b1, int first, int last)
+{
+    extern __shared__ unsigned char rs_raw[];
+    __shared__ __align__(8) uint64_t full_all[kRsWarps][kIsStages];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int wg = blockIdx.x * kRsWarps + warp;  // global (component, row block) index
+    if (wg >= 3 * s.nb) return;                   // no block-wide synchronisation below
+    unsigned char* buf = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(rs_raw) + 1023) &
+                                                          ~static_cast<uintptr_t>(1023)) +
+                         warp * kIsStages * kRsBox;
+    uint64_t* full = full_all[warp];
+    const int c = wg / s.nb;
+    const int rb = wg - c * s.nb;
+    const int i = rb * kBlock + lane;  // < npad
+    const int row0 = c * s.npad + rb * kBlock;
+    const int x0 = b0 * kBlock;
+    const int nq = (b1 - b0) * (kBlock / RsTerm<double>::kBoxCols);  // 16-column boxes
+    if (lane == 0) {
+        for (int k = 0; k < kIsStages; ++k) tma::mbar_init(&full[k], 1);
+        tma::fence_barrier_init();
+        for (int q = 0; q < nq && q < kIsStages; ++q) rs_issue<double, 1, kIsStages>(buf, full, &map, q, x0, row0);
+    }
+    __syncwarp();
+    // stage index of box q with kIsStages buffers
+    auto stage_buf = [&](int q) { return buf + (q % kIsStages) * kRsBox; };
+
+    const bool live = i < s.n;
+    double slow = first ? 0.0 : s.acc.c[c][i];  // the sum whenever run holds no frame
+    xs::Run run = xs::from_double(slow);
+    double ta = first ? 0.0 : s.aacc.c[c][i];
+    const size_t plane = (size_t)s.npad * s.npad;
+    const uint32_t* mrow = s.cmask + (size_t)i * s.nb;
+    const double* trow = s.torqbuf + c * plane + (size_t)i * s.npad;
+    uint32_t wnext = b1 > b0 ? mrow[b0] : 0u;
+
+    uint4 cur[8], nxt[8];
+    int waited = 0;
+    bool ok = nq <= 0 || __all_sync(0xffffffffu, tma::mbar_wait(&full[0], 0));
+    if (ok && nq > 0) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) cur[k] = rs_chunk(buf, lane, k);
+        waited = 1;
+    }
+    for (int q = 0; ok && q < nq; ++q) {
+        const xs::Run r0 = run;
+        float s32 = xs::shadow_of(run);
+        uint32_t bad = 0;
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            xs::step(run, s32, bad, is_lo(cur[k]));
+            xs::step(run, s32, bad, is_hi(cur[k]));
+        }
+        __syncwarp();  // every lane has box q in registers: its buffer is free
+        if (lane == 0 && q + kIsStages < nq) {
+            tma::fence_proxy_async();
+            rs_issue<double, 1, kIsStages>(buf, full, &map, q + kIsStages, x0, row0);
+        }
+#pragma unroll
+        for (int k = 2; k < 4; ++k) {
+            xs::step(run, s32, bad, is_lo(cur[k]));
+            xs::step(run, s32, bad, is_hi(cur[k]));
+        }
+        bool have_next = false;
+        if (q + 1 < nq) {
+            ok = __all_sync(0xffffffffu, tma::mbar_wait(&full[(q + 1) % kIsStages], ((q + 1) / kIsStages) & 1));
+            have_next = ok;
+        }
+#pragma unroll
+        for (int k = 4; k < 6; ++k) {
+            xs::step(run, s32, bad, is_lo(cur[k]));
+            xs::step(run, s32, bad, is_hi(cur[k]));
+        }
+        if (have_next) {
+#pragma unroll
+            for (int k = 0; k < 8; ++k) nxt[k] = rs_chunk(stage_buf(q + 1), lane, k);
+            waited = q + 2;
+        }
+#pragma unroll
+        for (int k = 6; k < 8; ++k) {
+            xs::step(run, s32, bad, is_lo(cur[k]));
+            xs::step(run, s32, bad, is_hi(cur[k]));
+        }
+        if (__any_sync(0xffffffffu, bad != 0 && live)) {
+            if (bad != 0) {  // repeat the chunk with FP64 additions
+                double v = r0.q == xs::kNoFrame ? slow : xs::to_double(r0);
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    v += __longlong_as_double((long long)is_lo(cur[k]));
+                    v += __longlong_as_double((long long)is_hi(cur[k]));
+                }
+                slow = v;
+                run = xs::from_double(v);
+            }
+        }
+        if (q & 1) {  // partner block Y complete: its torque terms, contact partners ascending
+            const int Y = b0 + (q >> 1);
+            uint32_t wd = wnext;
+            if (Y + 1 < b1) wnext = mrow[Y + 1];
+            while (wd) {
+                const int bit = __ffs(wd) - 1;
+                wd &= wd - 1;
+                ta += trow[Y * kBlock + bit];
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 8; ++k) cur[k] = nxt[k];
+    }
+    if (!ok) {
+        const int issued = min(nq, waited + kIsStages);
+        for (int qq = waited; qq < issued; ++qq) tma::mbar_wait(&full[qq % kIsStages], (qq / kIsStages) & 1);
+        if (lane == 0) atomicOr(s.status, kStatusWaitTimeoutBit);
+        return;
+    }
+    if (!live) return;
+    const double fa = run.q == xs::kNoFrame ? slow : xs::to_double(run);
+    s.acc.c[c][i] = fa;
+    s.aacc.c[c][i] = ta;
+    if (!last) return;
+    const double dt = s.sc->dt;
+    const double v = s.velh.c[c][i] + (.5 * fa) * dt;  // :265
+    const double wv = s.wh.c[c][i] + (.5 * ta) * dt;   // :266
+    s.vel.c[c][i] = v;
+    s.w.c[c][i] = wv;
+    if (!isfinite(v) || !isfinite(wv) || !isfinite(s.pos.c[c][i])) atomicOr(s.status, 1u);
+}
+
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
 {
     static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
@@ -258,14 +413,20 @@ bool make_pair_map(const System& s, CUtensorMap* map)
            cudaFuncSetAttribute(rowsum_tma_kernel<double, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 RsStage<1>::kSmem) == cudaSuccess &&
            cudaFuncSetAttribute(rowsum_tma_kernel<double, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                RsStage<2>::kSmem) == cudaSuccess;
+                                RsStage<2>::kSmem) == cudaSuccess &&
+           cudaFuncSetAttribute(rowsum_int_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kIsSmem) ==
+               cudaSuccess;
 }
 
 template <typename T>
 void launch_rowsum_tma(const System& s, const CUtensorMap& map, int b0, int b1, int first, int last, int num_sms,
-                       cudaStream_t st)
+                       bool int_adds, cudaStream_t st)
 {
     const int ctas = (3 * s.nb + kRsWarps - 1) / kRsWarps;
+    if (int_adds) {
+        rowsum_int_kernel<<<ctas, 32 * kRsWarps, kIsSmem, st>>>(s, map, b0, b1, first, last);
+        return;
+    }
     // two-box stages while every warp fits at 4 CTAs (8 warps) per SM and the
     // partner range is whole stages; one-box stages otherwise
     const bool wide = ctas <= 4 * num_sms && (RsTerm<T>::kBoxCols * 2 <= kBlock || (b1 - b0) % 2 == 0);
@@ -275,6 +436,7 @@ void launch_rowsum_tma(const System& s, const CUtensorMap& map, int b0, int b1, 
         rowsum_tma_kernel<T, 1><<<ctas, 32 * kRsWarps, RsStage<1>::kSmem, st>>>(s, map, b0, b1, first, last);
 }
 
-template void launch_rowsum_tma<double>(const System&, const CUtensorMap&, int, int, int, int, int, cudaStream_t);
+template void launch_rowsum_tma<double>(const System&, const CUtensorMap&, int, int, int, int, int, bool,
+                                         cudaStream_t);
 
 }  // namespace sl

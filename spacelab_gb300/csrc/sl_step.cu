@@ -409,10 +409,10 @@ void launch_energy(const System& s, cudaStream_t st)
 }
 
 static void launch_rowsum(const System& s, cudaStream_t st, const CUtensorMap* map, int b0, int b1, int first,
-                          int last, int num_sms)
+                          int last, int num_sms, bool int_adds)
 {
     if (map)
-        launch_rowsum_tma<double>(s, *map, b0, b1, first, last, num_sms, st);
+        launch_rowsum_tma<double>(s, *map, b0, b1, first, last, num_sms, int_adds, st);
     else
         rowsum_kernel<<<(3 * s.n + kRowThreads - 1) / kRowThreads, kRowThreads, 0, st>>>(s, b0, b1, first, last);
 }
@@ -429,7 +429,7 @@ static void launch_pair_columns(const System& s, bool write, int num_sms, cudaSt
 }
 
 void launch_step(const System& s, bool write, int num_sms, cudaStream_t st, StepTimers* tm, const StepOverlap* ov,
-                 const CUtensorMap* map)
+                 const CUtensorMap* map, bool int_adds)
 {
     launch_drift(s, st);
     if (tm) cudaEventRecord(tm->ev[0], st);
@@ -438,13 +438,13 @@ void launch_step(const System& s, bool write, int num_sms, cudaStream_t st, Step
     if (np <= 1) {
         launch_pair_columns(s, write, num_sms, st, 0, s.nb, 0);
         if (tm) cudaEventRecord(tm->ev[1], st);
-        launch_rowsum(s, st, map, 0, s.nb, 1, 1, num_sms);
+        launch_rowsum(s, st, map, 0, s.nb, 1, 1, num_sms, int_adds);
     } else {
         for (int p = 0; p < np; ++p) {
             launch_pair_columns(s, write, num_sms, st, cb[p], cb[p + 1], p);
             cudaEventRecord(ov->phase[p], st);
             cudaStreamWaitEvent(ov->side, ov->phase[p], 0);
-            launch_rowsum(s, ov->side, map, cb[p], cb[p + 1], p == 0, p == np - 1, num_sms);
+            launch_rowsum(s, ov->side, map, cb[p], cb[p + 1], p == 0, p == np - 1, num_sms, int_adds);
         }
         if (tm) cudaEventRecord(tm->ev[1], st);
         cudaEventRecord(ov->join, ov->side);

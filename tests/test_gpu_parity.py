@@ -247,6 +247,51 @@ def test_pipelined_step_matches_sequential(n):
         assert np.array_equal(sa[key], sb[key]), key
 
 
+@pytest.mark.parametrize("case", ["dense1000", "poly3000", "pipelined300"])
+def test_rowsum_methods_bit_identical(case):
+    """The row sums' FP64 additions on the integer pipe (the default) and on
+    the FP64 unit give the same state bit for bit, over single steps and the
+    graph-captured looper, with contacts, unequal radii and the pipelined
+    step; and both equal the oracle."""
+    if case == "dense1000":
+        c = contact_case(1000, 77)
+    elif case == "poly3000":
+        g = configs.build_cluster(3000, 3000, sigma_v=1e-2, sigma_ln=0.2)
+        kin, kout, dt = configs.spring_and_dt(float(g.R.max()), float(g.m.min()), 1.0)
+        c = {"pos": g.pos, "vel": g.vel, "w": g.w, "R": g.R, "m": g.m, "moi": g.moi, "dt": dt, "kin": kin,
+             "kout": kout}
+    else:
+        c = contact_case(300, 9)
+    a, b = _gpu(c), _gpu(c)
+    a.set_rowsum("int")
+    b.set_rowsum("fp64")
+    if case == "pipelined300":
+        a.set_overlap(True)
+        b.set_overlap(True)
+    o = _oracle(c)
+    a.init_conditions(); b.init_conditions(); o.init()
+    for step in range(1, 11):
+        a.sim_one_step(step % 5 == 0)
+        b.sim_one_step(step % 5 == 0)
+        o.step(step % 5 == 0)
+    sa, sb, so = _state(a), _state(b), o.state()
+    for key in STATE_KEYS:
+        assert np.array_equal(sa[key], sb[key]), key
+        assert np.array_equal(sa[key], so[key]), key
+    a.sim_looper(steps=30, skip=10, first_step=11)
+    b.sim_looper(steps=30, skip=10, first_step=11)
+    sa, sb = _state(a), _state(b)
+    for key in STATE_KEYS:
+        assert np.array_equal(sa[key], sb[key]), key
+
+
+def test_rowsum_method_is_exact_mode_only():
+    c = contact_case(64, 5)
+    s = _gpu(c, "mixed_df")
+    with pytest.raises(SpaceLabError):
+        s.set_rowsum("fp64")
+
+
 @pytest.mark.parametrize("mode", ["mixed", "mixed_df"])
 def test_mixed_mode_has_no_pipelined_step(mode):
     c = contact_case(64, 5)
