@@ -10,9 +10,10 @@
 // segments; the last segment does pass 3 (:263-267).  FP64 terms are added
 // in FP64 (the reference's own additions).
 //
-// Layout: one warp per (component, 32-row block), lane = row, kRsWarps
-// independent warps per CTA so that the warps and their FP64 add chains
-// spread over the SM's sub-partitions.  A stage of a warp's pipeline is one
+// Layout: one warp per (component, 32-row block), lane = row, one warp per
+// CTA, so that the block scheduler spreads the warps evenly: at N=5000 the
+// 471 warps land 3 or 4 to an SM (with two-warp CTAs, 84 SMs took 4 and 68
+// took 2; 0.2307 -> 0.2283 ms, and 2.62 -> 2.47 ms at N=20000).  A stage of a warp's pipeline is one
 // TMA box: the warp's 32 rows x 128 bytes (16 doubles or 32 floats), stored
 // with the 128-byte swizzle so that the lanes' 16-byte reads of their own
 // rows fall in distinct bank groups (4 wavefronts per 512 bytes, the
@@ -44,7 +45,7 @@ namespace sl {
 namespace {
 
 constexpr int kRsStages = 3;
-constexpr int kRsWarps = 2;
+constexpr int kRsWarps = 1;  // warps per CTA
 constexpr int kRsBox = kBlock * 128;  // one 128-byte-wide box of 32 rows
 
 // BPS boxes per stage: 2 when a system's warps are few (each stage wait then
@@ -102,7 +103,7 @@ __device__ __forceinline__ uint4 rs_chunk(const unsigned char* stage, int lane, 
 }
 
 template <typename T, int BPS>
-__global__ void __launch_bounds__(32 * kRsWarps, 8 / BPS) rowsum_tma_kernel(const __grid_constant__ System s,
+__global__ void __launch_bounds__(32 * kRsWarps, 16 / BPS) rowsum_tma_kernel(const __grid_constant__ System s,
                                                                             const __grid_constant__ CUtensorMap map,
                                                                             int b0, int b1, int first, int last)
 {
@@ -427,9 +428,9 @@ void launch_rowsum_tma(const System& s, const CUtensorMap& map, int b0, int b1, 
         rowsum_int_kernel<<<ctas, 32 * kRsWarps, kIsSmem, st>>>(s, map, b0, b1, first, last);
         return;
     }
-    // two-box stages while every warp fits at 4 CTAs (8 warps) per SM and the
-    // partner range is whole stages; one-box stages otherwise
-    const bool wide = ctas <= 4 * num_sms && (RsTerm<T>::kBoxCols * 2 <= kBlock || (b1 - b0) % 2 == 0);
+    // two-box stages while every warp fits at 8 warps per SM and the partner
+    // range is whole stages; one-box stages otherwise
+    const bool wide = 3 * s.nb <= 8 * num_sms && (RsTerm<T>::kBoxCols * 2 <= kBlock || (b1 - b0) % 2 == 0);
     if (wide)
         rowsum_tma_kernel<T, 2><<<ctas, 32 * kRsWarps, RsStage<2>::kSmem, st>>>(s, map, b0, b1, first, last);
     else
