@@ -11,7 +11,8 @@ pair evaluated per step, N(N-1)/2 per step.
 Prints one JSON line (rank 0).  `value` is device-resident throughput (state
 in HBM, CUDA events on the library's stream) over steps inside the
 collision's impact; `e2e` is the same metric through the C ABI from pinned
-host buffers, with the state uploaded and downloaded every step; `roofline`
+host buffers, the state read from them and written back every step
+(sl_step_host); `roofline`
 reports the pair kernel against the FP64 pipe (exact and mixed) or the FP32
 pipe (mixed_df); `cpu_baseline` times the reference's own step (compiled
 from its sources, one thread) on a bounded sample on this host.
@@ -571,8 +572,10 @@ def _read_profile_traffic():
 
 
 def run_e2e(sim, w, steps: int, first_step: int = 1) -> dict:
-    """Host-authoritative use of the drop-in: each step uploads the state from
-    pinned host buffers, runs sim_one_step on the GPU and downloads it."""
+    """Host-authoritative use of the drop-in: every step reads the state from
+    pinned host buffers, runs sim_one_step on the GPU and writes the new state
+    back into them (sl_step_host: the exchange and the step in one call, one
+    wait for the GPU)."""
     import ctypes
     import torch
     from spacelab_gb300 import _lib
@@ -586,9 +589,9 @@ def run_e2e(sim, w, steps: int, first_step: int = 1) -> dict:
     h = sim.handle
     # the host buffers stay put: their pointers are formed once, as a C
     # caller would hold them.  The state is the end of a step, so the
-    # previous-step positions that choose kin/kout are the uploaded ones
-    # (pos_prev NULL), as the reference's `distances` hold the pair distances
-    # of the current positions between steps.
+    # previous-step positions that choose kin/kout are the current ones, as
+    # the reference's `distances` hold the pair distances of the current
+    # positions between steps.
     P = _lib.dptr
     pp, pv, pw, pa, paa = P(pos), P(vel), P(wv), P(acc), P(aacc)
     e = _lib.Energy()
@@ -596,13 +599,12 @@ def run_e2e(sim, w, steps: int, first_step: int = 1) -> dict:
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for k in range(steps):
-        _lib.check(lib.sl_upload_resume(h, pp, pv, pw, pa, paa, None), "sl_upload_resume")
-        _lib.check(lib.sl_step(h, 1, int((first_step + k) % w.skip == 0), pe), "sl_step")
-        _lib.check(lib.sl_download(h, pp, pv, pw, pa, paa), "sl_download")
+        _lib.check(lib.sl_step_host(h, pp, pv, pw, pa, paa, int((first_step + k) % w.skip == 0), pe),
+                   "sl_step_host")
     el = time.perf_counter() - t0
     return {"value": w.pairs_per_step * steps / el, "unit": UNIT, "h2d_bytes_per_step": 5 * 3 * n * 8,
             "d2h_bytes_per_step": 5 * 3 * n * 8, "steps": steps, "first_step": first_step,
-            "api": "sl_upload_resume + sl_step(1) + sl_download per step"}
+            "api": "sl_step_host per step: reads pos, vel, w, acc, aacc from pinned host arrays, steps, writes them back"}
 
 
 # --------------------------------------------------- mixed vs FP64 report --

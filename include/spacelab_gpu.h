@@ -148,6 +148,20 @@ int sl_run(sl_handle* h, int first_step, int last_step, int skip, sl_energy* row
  * NULL): pos, vel, w, acc, aacc as vec3[n]. */
 int sl_download(sl_handle* h, double* pos, double* vel, double* w, double* acc, double* aacc);
 
+/* One reference step on a state the caller keeps on the host: the drop-in
+ * for sim_one_step(write) (ColliderSingleCore.cpp:78-288) when the host owns
+ * O.pos/vel/w/acc/aacc and may change them between steps.  Reads the five
+ * vec3[n] arrays (the end of the caller's previous step; its previous-step
+ * positions are taken as pos, as the reference's `distances` hold the
+ * current positions' pair distances between steps), runs the step, and
+ * writes the new state back into the same arrays; a write step's totals go
+ * to *out (may be NULL).  The same bits as sl_upload_resume(h, pos, vel, w,
+ * acc, aacc, NULL) + sl_step(h, 1, write, out) + sl_download(h, pos, vel,
+ * w, acc, aacc), with one wait for the GPU instead of three.  Requires
+ * sl_upload (R, m, moi) first; pos, vel, w, acc, aacc non-NULL. */
+int sl_step_host(sl_handle* h, double* pos, double* vel, double* w, double* acc, double* aacc, int write,
+                 sl_energy* out);
+
 /* Contact pairs (A > B, overlap R[A]+R[B]-|pos[B]-pos[A]| > 0) found by the
  * last force pass, in the reference's loop order (A ascending, then B
  * ascending; ColliderSingleCore.cpp:100-119).  Writes min(count, max_pairs)

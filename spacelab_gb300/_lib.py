@@ -69,6 +69,7 @@ _PROTOS = [
     ("sl_run", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(Energy),
                               ctypes.c_int, _c_int_p]),
     ("sl_download", ctypes.c_int, [ctypes.c_void_p] + [_c_double_p] * 5),
+    ("sl_step_host", ctypes.c_int, [ctypes.c_void_p] + [_c_double_p] * 5 + [ctypes.c_int, ctypes.POINTER(Energy)]),
     ("sl_contacts", ctypes.c_int, [ctypes.c_void_p, _c_int_p, ctypes.c_long, ctypes.POINTER(ctypes.c_long)]),
     ("sl_stream", ctypes.c_void_p, [ctypes.c_void_p]),
     ("sl_set_overlap", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),

@@ -184,6 +184,19 @@ class GpuStep:
             return e
         return None
 
+    def sim_one_step_host(self, write_step: bool) -> Energy | None:
+        """One step on the state held in the group's host arrays
+        (sl_step_host): they are read, stepped and overwritten in place; on
+        write steps the totals are added to the group's PE/KE/mom/ang_mom."""
+        g = self.group
+        e = Energy()
+        check(self._lib.sl_step_host(self._h, dptr(g.pos), dptr(g.vel), dptr(g.w), dptr(g.acc), dptr(g.aacc),
+                                     int(bool(write_step)), ctypes.byref(e)), "sl_step_host")
+        if write_step:
+            g.add_totals(e)
+            return e
+        return None
+
     def step(self, nsteps: int, write_last: bool = False) -> Energy | None:
         e = Energy()
         check(self._lib.sl_step(self._h, int(nsteps), int(bool(write_last)), ctypes.byref(e)), "sl_step")

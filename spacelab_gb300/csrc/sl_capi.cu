@@ -384,10 +384,14 @@ int sl_upload(sl_handle* h, const double* pos, const double* vel, const double* 
     return SL_OK;
 }
 
-int sl_upload_resume(sl_handle* h, const double* pos, const double* vel, const double* w, const double* acc,
-                     const double* aacc, const double* pos_prev)
+namespace {
+
+// The exchange of sl_upload_resume, enqueued on the handle's stream without
+// waiting: the finite check on the host, then the staging kernel (reading
+// each array in place where the GPU can reach it, else through a copy).
+int enqueue_resume(sl_handle* h, const double* pos, const double* vel, const double* w, const double* acc,
+                   const double* aacc, const double* pos_prev)
 {
-    if (int r = check_handle(h)) return r;
     if (!pos || !vel || !w) return fail(SL_ERR_ARG, "pos, vel or w is NULL");
     const int n = h->sys.n;
     if (!all_finite(pos, 3 * (size_t)n) || !all_finite(vel, 3 * (size_t)n) || !all_finite(w, 3 * (size_t)n))
@@ -415,6 +419,48 @@ int sl_upload_resume(sl_handle* h, const double* pos, const double* vel, const d
     sl::launch_stage_in(h->sys, views, dst, present, h->stream);
     SL_CUDA(cudaGetLastError());
     SL_CUDA(cudaMemsetAsync(h->sys.status, 0, sizeof(unsigned int), h->stream));
+    return SL_OK;
+}
+
+// The exchange of sl_download, enqueued without waiting.  outs[k] that the
+// GPU cannot reach are written through the staging area and a copy, which
+// the caller's stream synchronisation completes.
+int enqueue_download(sl_handle* h, double* pos, double* vel, double* w, double* acc, double* aacc)
+{
+    double* outs[5] = {pos, vel, w, acc, aacc};
+    const size_t np = h->sys.npad;
+    const int n = h->sys.n;
+    unsigned want = 0;
+    for (int k = 0; k < 5; ++k)
+        if (outs[k]) want |= 1u << k;
+    sl::Vec3Soa* src[6];
+    stage_arrays(h, src);
+    double* views[6] = {};
+    bool staged[5] = {};
+    for (int k = 0; k < 5; ++k)
+        if (outs[k]) {
+            views[k] = const_cast<double*>(device_view(h, outs[k]));
+            if (!views[k]) {
+                views[k] = h->d_stage + (size_t)k * 3 * np;
+                staged[k] = true;
+            }
+        }
+    sl::launch_stage_out(h->sys, views, src, want, h->stream);
+    SL_CUDA(cudaGetLastError());
+    for (int k = 0; k < 5; ++k)
+        if (staged[k])
+            SL_CUDA(cudaMemcpyAsync(outs[k], views[k], 3 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost,
+                                    h->stream));
+    return SL_OK;
+}
+
+}  // namespace
+
+int sl_upload_resume(sl_handle* h, const double* pos, const double* vel, const double* w, const double* acc,
+                     const double* aacc, const double* pos_prev)
+{
+    if (int r = check_handle(h)) return r;
+    if (int r = enqueue_resume(h, pos, vel, w, acc, aacc, pos_prev)) return r;
     SL_CUDA(cudaStreamSynchronize(h->stream));
     h->forces_ready = (acc != nullptr && aacc != nullptr);
     return SL_OK;
@@ -507,33 +553,25 @@ int sl_run(sl_handle* h, int first_step, int last_step, int skip, sl_energy* row
 int sl_download(sl_handle* h, double* pos, double* vel, double* w, double* acc, double* aacc)
 {
     if (int r = check_handle(h)) return r;
-    double* outs[5] = {pos, vel, w, acc, aacc};
-    const size_t np = h->sys.npad;
-    const int n = h->sys.n;
-    unsigned want = 0;
-    for (int k = 0; k < 5; ++k)
-        if (outs[k]) want |= 1u << k;
-    sl::Vec3Soa* src[6];
-    stage_arrays(h, src);
-    // written where the GPU can reach the caller's array, else staged and copied
-    double* views[6] = {};
-    bool staged[5] = {};
-    for (int k = 0; k < 5; ++k)
-        if (outs[k]) {
-            views[k] = const_cast<double*>(device_view(h, outs[k]));
-            if (!views[k]) {
-                views[k] = h->d_stage + (size_t)k * 3 * np;
-                staged[k] = true;
-            }
-        }
-    sl::launch_stage_out(h->sys, views, src, want, h->stream);
-    SL_CUDA(cudaGetLastError());
-    for (int k = 0; k < 5; ++k)
-        if (staged[k])
-            SL_CUDA(cudaMemcpyAsync(outs[k], views[k], 3 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost,
-                                    h->stream));
+    if (int r = enqueue_download(h, pos, vel, w, acc, aacc)) return r;
     SL_CUDA(cudaStreamSynchronize(h->stream));
     return SL_OK;
+}
+
+int sl_step_host(sl_handle* h, double* pos, double* vel, double* w, double* acc, double* aacc, int write,
+                 sl_energy* out)
+{
+    if (int r = check_handle(h)) return r;
+    if (!h->uploaded) return fail(SL_ERR_STATE, "sl_upload first");
+    if (!acc || !aacc) return fail(SL_ERR_ARG, "acc or aacc is NULL");
+    // the state at the end of the caller's previous step: the previous-step
+    // positions are the current ones (pos_prev NULL), as the reference's
+    // `distances` hold the current positions' pair distances between steps
+    if (int r = enqueue_resume(h, pos, vel, w, acc, aacc, nullptr)) return r;
+    h->forces_ready = true;
+    if (int r = enqueue_step(h, write != 0)) return r;
+    if (int r = enqueue_download(h, pos, vel, w, acc, aacc)) return r;
+    return fetch_energy_and_status(h, out, write != 0);
 }
 
 int sl_contacts(sl_handle* h, int* pairs, long max_pairs, long* count)

@@ -325,6 +325,34 @@ def test_resume_matches_continuous_run():
         assert np.array_equal(sa[key], sb[key]), key
 
 
+def test_step_host_matches_resident_steps_and_oracle():
+    """sl_step_host (state on the host, read and overwritten every step)
+    gives the device-resident run's states and totals bit for bit, step after
+    step, and the oracle's; an array it cannot read fails cleanly."""
+    c = contact_case(300, 41)
+    a, b = _gpu(c), _gpu(c)
+    o = _oracle(c)
+    a.init_conditions(); b.init_conditions(); o.init()
+    b.download()  # the host copy b's steps work on
+    for step in range(1, 21):
+        write = step % 5 == 0
+        ea = a.sim_one_step(write)
+        eb = b.sim_one_step_host(write)
+        o.step(write)
+        if write:
+            assert ea.as_array().tolist() == eb.as_array().tolist()
+        sa = _state(a)
+        for key in STATE_KEYS:
+            assert np.array_equal(sa[key], getattr(b.group, key)), (step, key)
+    so = o.state()
+    for key in STATE_KEYS:
+        assert np.array_equal(getattr(b.group, key), so[key]), key
+    g = b.group
+    rc = _lib.lib().sl_step_host(b.handle, _lib.dptr(g.pos), _lib.dptr(g.vel), _lib.dptr(g.w), None,
+                                 _lib.dptr(g.aacc), 0, None)
+    assert rc == _lib.SL_ERR_ARG
+
+
 def test_reciprocal_division_is_ieee_exact():
     lib = _lib.lib()
     rng = np.random.default_rng(0)
