@@ -31,6 +31,7 @@ int main(void)
     printf("%s\n", sl_last_error());
     if (sl_destroy(NULL) != SL_OK) return 12;
     if (sl_step(NULL, 1, 0, NULL) != SL_ERR_ARG) return 13;
+    if (sl_step_host(NULL, NULL, NULL, NULL, NULL, NULL, 0, NULL) != SL_ERR_ARG) return 16;
     double kin = 0, kout = 0, dt = 0;
     if (slh_spring_and_dt(1e-4, 7e-12, 10.0, 1.7, 0.4096, 50.0, &kin, &kout, &dt) != 0) return 14;
     if (!(kin > 0 && kout > 0 && dt > 0)) return 15;
