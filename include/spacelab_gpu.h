@@ -158,7 +158,10 @@ int sl_download(sl_handle* h, double* pos, double* vel, double* w, double* acc, 
  * to *out (may be NULL).  The same bits as sl_upload_resume(h, pos, vel, w,
  * acc, aacc, NULL) + sl_step(h, 1, write, out) + sl_download(h, pos, vel,
  * w, acc, aacc), with one wait for the GPU instead of three.  Requires
- * sl_upload (R, m, moi) first; pos, vel, w, acc, aacc non-NULL. */
+ * sl_upload (R, m, moi) first; pos, vel, w, acc, aacc non-NULL.  A NaN or
+ * Inf in pos, vel or w returns SL_ERR_ARG and leaves the five arrays as they
+ * were (*out is then undefined); the handle's device copy of the state is
+ * undefined until the next successful upload or sl_step_host. */
 int sl_step_host(sl_handle* h, double* pos, double* vel, double* w, double* acc, double* aacc, int write,
                  sl_energy* out);
 

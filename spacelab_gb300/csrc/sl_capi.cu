@@ -141,6 +141,8 @@ int fetch_energy_and_status(sl_handle* h, sl_energy* out, bool want_energy)
             out->ang_mom[k] = h->h_energy[5 + k];
         }
     }
+    if (*h->h_status & sl::kStatusInputNonFiniteBit)
+        return fail(SL_ERR_ARG, "non-finite position, velocity or spin in input");
     if (*h->h_status & sl::kStatusWaitTimeoutBit)
         return fail(SL_ERR_TIMEOUT, "a row-sum kernel's bounded wait for its TMA copies ran out");
     if (*h->h_status) return fail(SL_ERR_NONFINITE, "state became non-finite (NaN/Inf position, velocity or spin)");
@@ -387,15 +389,20 @@ int sl_upload(sl_handle* h, const double* pos, const double* vel, const double* 
 namespace {
 
 // The exchange of sl_upload_resume, enqueued on the handle's stream without
-// waiting: the finite check on the host, then the staging kernel (reading
-// each array in place where the GPU can reach it, else through a copy).
+// waiting: the status word cleared, then the staging kernel (reading each
+// array in place where the GPU can reach it, else through a copy).  The
+// finite check of pos, vel and w runs on the host before anything is
+// enqueued, or, with device_check, in the staging kernel itself
+// (kStatusInputNonFiniteBit, read by the caller after its wait).
 int enqueue_resume(sl_handle* h, const double* pos, const double* vel, const double* w, const double* acc,
-                   const double* aacc, const double* pos_prev)
+                   const double* aacc, const double* pos_prev, bool device_check)
 {
     if (!pos || !vel || !w) return fail(SL_ERR_ARG, "pos, vel or w is NULL");
     const int n = h->sys.n;
-    if (!all_finite(pos, 3 * (size_t)n) || !all_finite(vel, 3 * (size_t)n) || !all_finite(w, 3 * (size_t)n))
+    if (!device_check &&
+        (!all_finite(pos, 3 * (size_t)n) || !all_finite(vel, 3 * (size_t)n) || !all_finite(w, 3 * (size_t)n)))
         return fail(SL_ERR_ARG, "non-finite position, velocity or spin in input");
+    SL_CUDA(cudaMemsetAsync(h->sys.status, 0, sizeof(unsigned int), h->stream));
     const size_t np = h->sys.npad;
     // the staging kernel reads each array where the GPU can reach it, else
     // from a copy in the device staging area; absent acc/aacc are zero, an
@@ -416,16 +423,18 @@ int enqueue_resume(sl_handle* h, const double* pos, const double* vel, const dou
         }
     sl::Vec3Soa* dst[6];
     stage_arrays(h, dst);
-    sl::launch_stage_in(h->sys, views, dst, present, h->stream);
+    sl::launch_stage_in(h->sys, views, dst, present, h->stream, device_check ? 7u : 0u);
     SL_CUDA(cudaGetLastError());
-    SL_CUDA(cudaMemsetAsync(h->sys.status, 0, sizeof(unsigned int), h->stream));
     return SL_OK;
 }
 
 // The exchange of sl_download, enqueued without waiting.  outs[k] that the
 // GPU cannot reach are written through the staging area and a copy, which
-// the caller's stream synchronisation completes.
-int enqueue_download(sl_handle* h, double* pos, double* vel, double* w, double* acc, double* aacc)
+// the caller's stream synchronisation completes.  guard (only where the GPU
+// reaches every array, so that nothing goes through a copy): nothing is
+// written once the staging kernel found a non-finite input.
+int enqueue_download(sl_handle* h, double* pos, double* vel, double* w, double* acc, double* aacc,
+                     bool guard = false)
 {
     double* outs[5] = {pos, vel, w, acc, aacc};
     const size_t np = h->sys.npad;
@@ -445,7 +454,7 @@ int enqueue_download(sl_handle* h, double* pos, double* vel, double* w, double* 
                 staged[k] = true;
             }
         }
-    sl::launch_stage_out(h->sys, views, src, want, h->stream);
+    sl::launch_stage_out(h->sys, views, src, want, h->stream, guard);
     SL_CUDA(cudaGetLastError());
     for (int k = 0; k < 5; ++k)
         if (staged[k])
@@ -460,7 +469,7 @@ int sl_upload_resume(sl_handle* h, const double* pos, const double* vel, const d
                      const double* aacc, const double* pos_prev)
 {
     if (int r = check_handle(h)) return r;
-    if (int r = enqueue_resume(h, pos, vel, w, acc, aacc, pos_prev)) return r;
+    if (int r = enqueue_resume(h, pos, vel, w, acc, aacc, pos_prev, false)) return r;
     SL_CUDA(cudaStreamSynchronize(h->stream));
     h->forces_ready = (acc != nullptr && aacc != nullptr);
     return SL_OK;
@@ -564,14 +573,24 @@ int sl_step_host(sl_handle* h, double* pos, double* vel, double* w, double* acc,
     if (int r = check_handle(h)) return r;
     if (!h->uploaded) return fail(SL_ERR_STATE, "sl_upload first");
     if (!acc || !aacc) return fail(SL_ERR_ARG, "acc or aacc is NULL");
-    // the state at the end of the caller's previous step: the previous-step
-    // positions are the current ones (pos_prev NULL), as the reference's
-    // `distances` hold the current positions' pair distances between steps
-    if (int r = enqueue_resume(h, pos, vel, w, acc, aacc, nullptr)) return r;
+    // The arrays hold the state at the end of the caller's previous step:
+    // the previous-step positions are the current ones (pos_prev NULL), as
+    // the reference's `distances` hold the current positions' pair distances
+    // between steps.  Where the GPU reaches all five arrays, the finite check
+    // of the input runs in the staging kernel and a rejected input is never
+    // written back; otherwise it runs on the host first.
+    bool reach = true;
+    for (const double* p : {static_cast<const double*>(pos), static_cast<const double*>(vel),
+                            static_cast<const double*>(w), static_cast<const double*>(acc),
+                            static_cast<const double*>(aacc)})
+        reach = reach && p && device_view(h, p) != nullptr;
+    if (int r = enqueue_resume(h, pos, vel, w, acc, aacc, nullptr, reach)) return r;
     h->forces_ready = true;
     if (int r = enqueue_step(h, write != 0)) return r;
-    if (int r = enqueue_download(h, pos, vel, w, acc, aacc)) return r;
-    return fetch_energy_and_status(h, out, write != 0);
+    if (int r = enqueue_download(h, pos, vel, w, acc, aacc, reach)) return r;
+    const int r = fetch_energy_and_status(h, out, write != 0);
+    if (r == SL_ERR_ARG) h->forces_ready = false;  // the device copy holds the rejected input
+    return r;
 }
 
 int sl_contacts(sl_handle* h, int* pairs, long max_pairs, long* count)

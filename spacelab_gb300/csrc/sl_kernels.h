@@ -30,10 +30,13 @@ void launch_derive(const System& s, cudaStream_t st);
 // or host memory the GPU reads and writes directly) <-> the SoA arrays
 // arr[k]: in, for the arrays whose bit is set in `present` (others: arr[5],
 // the previous positions, takes the positions; the rest zero); out, for the
-// arrays whose bit is set in `want`.
+// arrays whose bit is set in `want`.  check: arrays of `present` whose
+// non-finite values set kStatusInputNonFiniteBit; guard: stage_out writes
+// nothing once that bit is set.
 void launch_stage_in(const System& s, const double* const src[6], Vec3Soa* const arr[6], unsigned present,
-                     cudaStream_t st);
-void launch_stage_out(const System& s, double* const dst[6], Vec3Soa* const arr[6], unsigned want, cudaStream_t st);
+                     cudaStream_t st, unsigned check = 0);
+void launch_stage_out(const System& s, double* const dst[6], Vec3Soa* const arr[6], unsigned want, cudaStream_t st,
+                      bool guard = false);
 // map: a tensor map of the pair-term buffer (make_pair_map) selects the
 // TMA-streamed row sums; NULL the plain-load form.
 void launch_step(const System& s, bool write, int num_sms, cudaStream_t st, StepTimers* tm,
@@ -51,6 +54,9 @@ void launch_rowsum_tma(const System& s, const CUtensorMap& map, int b0, int b1, 
                        bool int_adds, cudaStream_t st);
 // Status bit set by a kernel whose bounded wait for a TMA copy ran out.
 constexpr unsigned kStatusWaitTimeoutBit = 2u;
+// Status bit set by stage_in for a non-finite value of a checked input array
+// (launch_stage_in's `check` mask); a guarded stage_out then writes nothing.
+constexpr unsigned kStatusInputNonFiniteBit = 0x40000000u;
 // The double-float mixed form (SL_MODE_MIXED_DF, sl_step_mixed.cu).
 void launch_step_mixed(const System& s, bool write, int num_sms, cudaStream_t st, StepTimers* tm);
 // The mixed form with FP64 displacements, overlaps and accumulation

@@ -319,25 +319,30 @@ struct StagePtrs {
 // may cross the CPU-GPU link -- and the gather / scatter falls on the SoA
 // arrays in HBM.
 __global__ void stage_in_kernel(const __grid_constant__ System s, const __grid_constant__ StagePtrs src,
-                                const __grid_constant__ StageArrays arr, unsigned present)
+                                const __grid_constant__ StageArrays arr, unsigned present, unsigned check)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 3 * s.npad) return;
     const int i = t / 3, c = t - 3 * (t / 3);
     const bool real = i < s.n;
+    bool finite = true;
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
         const int from = (k == 5 && !(present & 32u)) ? 0 : k;  // previous positions default to the positions
         const bool have = real && ((present >> from) & 1u);
-        arr.a[k].c[c][i] = have ? src.p[from][t] : 0.0;
+        const double v = have ? src.p[from][t] : 0.0;
+        if ((check >> k) & 1u) finite = finite && isfinite(v);
+        arr.a[k].c[c][i] = v;
     }
+    if (!finite) atomicOr(s.status, kStatusInputNonFiniteBit);
 }
 
 __global__ void stage_out_kernel(const __grid_constant__ System s, const __grid_constant__ StagePtrs dst,
-                                 const __grid_constant__ StageArrays arr, unsigned want)
+                                 const __grid_constant__ StageArrays arr, unsigned want, bool guard)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 3 * s.n) return;
+    if (guard && (*s.status & kStatusInputNonFiniteBit)) return;  // the caller's arrays stay as they were
     const int i = t / 3, c = t - 3 * (t / 3);
 #pragma unroll
     for (int k = 0; k < 6; ++k)
@@ -373,7 +378,7 @@ void launch_derive(const System& s, cudaStream_t st)
 }
 
 void launch_stage_in(const System& s, const double* const src[6], Vec3Soa* const arr[6], unsigned present,
-                     cudaStream_t st)
+                     cudaStream_t st, unsigned check)
 {
     StageArrays a;
     StagePtrs p;
@@ -381,10 +386,11 @@ void launch_stage_in(const System& s, const double* const src[6], Vec3Soa* const
         a.a[k] = *arr[k];
         p.p[k] = src[k];
     }
-    stage_in_kernel<<<(3 * s.npad + 255) / 256, 256, 0, st>>>(s, p, a, present);
+    stage_in_kernel<<<(3 * s.npad + 255) / 256, 256, 0, st>>>(s, p, a, present, check);
 }
 
-void launch_stage_out(const System& s, double* const dst[6], Vec3Soa* const arr[6], unsigned want, cudaStream_t st)
+void launch_stage_out(const System& s, double* const dst[6], Vec3Soa* const arr[6], unsigned want, cudaStream_t st,
+                      bool guard)
 {
     StageArrays a;
     StagePtrs p;
@@ -392,7 +398,7 @@ void launch_stage_out(const System& s, double* const dst[6], Vec3Soa* const arr[
         a.a[k] = *arr[k];
         p.p[k] = dst[k];
     }
-    stage_out_kernel<<<(3 * s.n + 255) / 256, 256, 0, st>>>(s, p, a, want);
+    stage_out_kernel<<<(3 * s.n + 255) / 256, 256, 0, st>>>(s, p, a, want, guard);
 }
 
 void launch_drift(const System& s, cudaStream_t st)

@@ -351,6 +351,21 @@ def test_step_host_matches_resident_steps_and_oracle():
     rc = _lib.lib().sl_step_host(b.handle, _lib.dptr(g.pos), _lib.dptr(g.vel), _lib.dptr(g.w), None,
                                  _lib.dptr(g.aacc), 0, None)
     assert rc == _lib.SL_ERR_ARG
+    # a NaN or Inf input is rejected and the arrays are left as they were;
+    # the next valid call steps as before
+    before = {k: getattr(g, k).copy() for k in STATE_KEYS}
+    for key, bad in (("pos", np.nan), ("vel", np.inf), ("w", -np.inf)):
+        getattr(g, key)[7, 1] = bad
+        with pytest.raises(SpaceLabError):
+            b.sim_one_step_host(False)
+        getattr(g, key)[7, 1] = before[key][7, 1]
+        for k in STATE_KEYS:
+            assert np.array_equal(getattr(g, k), before[k]), (key, k)
+    b.sim_one_step_host(False)
+    a.sim_one_step(False)
+    sa = _state(a)
+    for key in STATE_KEYS:
+        assert np.array_equal(sa[key], getattr(b.group, key)), key
 
 
 def test_reciprocal_division_is_ieee_exact():
