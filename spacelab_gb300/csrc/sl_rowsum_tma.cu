@@ -13,18 +13,19 @@
 // Layout: one warp per (component, 32-row block), lane = row, one warp per
 // CTA, so that the block scheduler spreads the warps evenly: at N=5000 the
 // 471 warps land 3 or 4 to an SM (with two-warp CTAs, 84 SMs took 4 and 68
-// took 2; 0.2307 -> 0.2283 ms, and 2.62 -> 2.47 ms at N=20000).  A stage of a warp's pipeline is one
-// TMA box: the warp's 32 rows x 128 bytes (16 doubles or 32 floats), stored
+// took 2; 0.2307 -> 0.2283 ms, and 2.62 -> 2.47 ms at N=20000).  A box of
+// the TMA pipeline is the warp's 32 rows x 128 bytes (16 doubles), stored
 // with the 128-byte swizzle so that the lanes' 16-byte reads of their own
 // rows fall in distinct bank groups (4 wavefronts per 512 bytes, the
-// minimum).  kRsStages boxes are in flight per warp; one lane issues the
+// minimum).  kRsStages stages are in flight per warp; one lane issues the
 // copies and every wait is bounded (sl_tma.cuh): a copy that does not land
 // sets status bit 2 and the warp returns after draining its other copies.
 // A stage is one box or two (RsStage): with one, the footprint (12 KB of
 // shared memory and at most 128 registers per thread) lets 16 warps share
 // an SM, so that the 3n/32 warps of a system of up to ~26,000 spheres run in
 // one wave; with two, each stage wait covers twice the adds, which pays when
-// the warps are few.
+// the warps are few.  The stage in registers and the next one alternate
+// between two register sets.
 //
 // Every entry of a row is added, the row's own column and the padding
 // columns included: those are never written and hold +0.0 (a handle's arena
