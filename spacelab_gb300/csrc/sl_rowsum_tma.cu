@@ -235,16 +235,16 @@ __global__ void __launch_bounds__(32 * kRsWarps, 16 / BPS) rowsum_tma_kernel(con
 // ---------------------------------------------------------------------------
 // rowsum_int_kernel: the same ordered sums with each FP64 addition computed
 // on the integer pipe (sl_sum_exact.cuh) instead of the FP64 unit
-// (SL_ROWSUM_INT).  On GB300 it is the slower of the two at N=5000 (0.38
-// against 0.23 ms): ~49 ALU instructions per addition at the ALU pipe's
-// half rate outweigh the FP64 unit's 64-76-cycle dependent adds.
+// (SL_ROWSUM_INT).  On GB300 it is the slower of the two at N=5000 (0.38-
+// 0.40 against 0.22 ms): ~49 ALU instructions per addition at the ALU
+// pipe's half rate outweigh the FP64 unit's 64-76-cycle dependent adds.
 //
 // Same mapping as rowsum_tma_kernel (one warp per (component, 32-row block),
 // lane = row, rows streamed in 16-column TMA boxes), and a box is one chunk
 // of 16 additions: the running sum at the chunk's start is kept, the 16
 // additions run in the frame form, and a lane whose fast path left its
-// domain (a binade prediction that failed, a jump of more than 8 binades, a
-// term larger than the new sum) repeats the chunk with FP64 additions.  Both
+// domain (a binade prediction that failed, a binade change outside -1..+8,
+// a term larger than the new sum) repeats the chunk with FP64 additions.  Both
 // paths give RN(s + t) at every addition, in the reference's order, so the
 // sums are the FP64 kernel's bit for bit.  Padding rows (i >= n, all terms
 // +0.0, never stored) take no part in the warp's vote, so their zero sums
