@@ -607,6 +607,27 @@ def run_e2e(sim, w, steps: int, first_step: int = 1) -> dict:
             "api": "sl_step_host per step: reads pos, vel, w, acc, aacc from pinned host arrays, steps, writes them back"}
 
 
+# ------------------------------------------------ FP64 add-chain latency --
+def run_fp64_latency_table() -> dict:
+    """Cycles per dependent FP64 add (sl_diag_fp64_add_latency) for 1-8
+    warps per SM and 8-32 active lanes per warp: what bounds the exact row
+    sums' chains."""
+    import ctypes
+    import torch
+    from spacelab_gb300 import _lib
+    torch.cuda.init()
+    lib = _lib.lib()
+    c = ctypes.c_double()
+    rows = []
+    for warps in (1, 2, 3, 4, 5, 6, 8):
+        for lanes in (8, 16, 24, 32):
+            _lib.check(lib.sl_diag_fp64_add_latency(warps, lanes, ctypes.byref(c)), "sl_diag_fp64_add_latency")
+            rows.append({"warps_per_sm": warps, "active_lanes": lanes, "cycles_per_add": round(c.value, 1),
+                         "lane_adds_per_clock_per_sm": round(warps * lanes / c.value, 3)})
+    return {"metric": "FP64 dependent-add latency", "unit": "cycles per add at the rated SM clock", "table": rows,
+            "gpu": torch.cuda.get_device_name(0)}
+
+
 # --------------------------------------------------- mixed vs FP64 report --
 def run_drift(args) -> dict:
     """Both mixed-precision forms against the FP64 form on the same seed:
@@ -821,6 +842,8 @@ def main(argv=None) -> int:
                     help="exact mode: the row sums' FP64 additions on the FP64 unit (default) or the integer pipe "
                          "(sl_set_rowsum); identical results")
     ap.add_argument("--workload", choices=WORKLOADS, default="aggregate_collision_n5000")
+    ap.add_argument("--fp64-latency-table", action="store_true",
+                    help="print the dependent FP64 add latency for 1-8 warps per SM and 8-32 active lanes")
     ap.add_argument("--drift-steps", type=int, default=0,
                     help="instead of the benchmark: run the mixed and the FP64 form side by side for this many "
                          "steps and report energy drift and trajectory error")
@@ -858,6 +881,9 @@ def main(argv=None) -> int:
         res = run_reference(args, rank, world)
         if res is not None:
             emit(res)
+        return 0
+    if args.fp64_latency_table:
+        emit(run_fp64_latency_table())
         return 0
     if args.drift_steps:
         emit(run_drift(args))
